@@ -1,0 +1,202 @@
+/*
+ * rsvdt.h -- C ABI of the GB300 RSVD-Delta-t time-stepping library.
+ *
+ * One context owns one GPU stream and every device buffer of one resolvent
+ * problem. It replaces the reference's PETSc-typed hot-path functions
+ * (AliFarghadan/RSVD-Delta-t, SourceCode/): the entry points below name the
+ * reference function each one stands in for.
+ *
+ * Conventions
+ *  - Complex values cross this interface as interleaved (re, im) doubles,
+ *    layout-compatible with C99 `double _Complex` and PETSc's complex
+ *    PetscScalar. "count complex values" means 2*count doubles.
+ *  - Spectral blocks (forcing F_hat, response Y_hat, modes U/V) use the
+ *    reference's layout: rows x (k*Nw_eff), column-major, column iw*k+ik
+ *    (frequency-major; SourceCode/CreateRandomMat.c:34,
+ *    SourceCode/PermuteMat.c:24-34), leading dimension `ld` >= rows.
+ *  - Sparse matrices are CSR with int64 row pointers and column indices
+ *    (PETSc 64-bit-index AIJ). Host arrays are caller-owned and copied.
+ *  - Every call returns an rsvdt_status; 0 is success. rsvdt_last_error()
+ *    gives the message of the last failure on that context. A context is
+ *    not thread-safe; separate contexts may be used from separate threads.
+ *  - There is no CPU fallback: without a usable GPU rsvdt_create fails with
+ *    RSVDT_ERR_CUDA.
+ */
+#ifndef RSVDT_H
+#define RSVDT_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  RSVDT_OK = 0,
+  RSVDT_ERR_ARG = 1,      /* invalid argument or size mismatch (SETERRQ PETSC_ERR_USER) */
+  RSVDT_ERR_IO = 2,       /* file could not be read or written */
+  RSVDT_ERR_OOM = 3,      /* device or host allocation failed */
+  RSVDT_ERR_CUDA = 4,     /* CUDA runtime error */
+  RSVDT_ERR_NOT_SPD = 5,  /* Cholesky of a Gram matrix failed (rank-deficient block) */
+  RSVDT_ERR_DIVERGED = 6, /* NaN or Inf in the state */
+  RSVDT_ERR_TIMEOUT = 7,  /* a bounded device wait gave up */
+  RSVDT_ERR_STATE = 8     /* call out of order (e.g. action before operator) */
+} rsvdt_status;
+
+typedef enum { RSVDT_ADJOINT = 0, RSVDT_DIRECT = 1 } rsvdt_dir;
+
+typedef enum {
+  RSVDT_PREC_C128 = 0, /* plain form: complex128 throughout */
+  RSVDT_PREC_C64 = 1   /* precision form: complex64 operator/state/stages, FP32
+                          accumulation; FP64 DFT, QR, SVD and spectral blocks */
+} rsvdt_precision;
+
+/* Weight / input / output matrices (SourceCode/Variables.h:69-80). */
+typedef enum {
+  RSVDT_W_F_SQRT_INV = 0, /* W_f^{-1/2}, Nb x Nb */
+  RSVDT_B = 1,            /* B, N x Nb */
+  RSVDT_C = 2,            /* C, Nc x N */
+  RSVDT_W_Q_SQRT = 3,     /* W_q^{1/2}, Nc x Nc */
+  RSVDT_W_Q_SQRT_INV = 4  /* W_q^{-1/2}, Nc x Nc */
+} rsvdt_weight;
+
+/* Mirrors RSVD_vars / TS_vars / Discounting (SourceCode/Variables.h:5-41)
+ * and the variables.yaml keys of the same names. */
+typedef struct {
+  int64_t k;               /* test vectors */
+  int64_t q;               /* power iterations */
+  int64_t Nw;              /* frequencies */
+  double w;                /* base frequency (multiplied by 2*pi when TwoPI) */
+  int32_t TwoPI;           /* bool */
+  double dt;               /* requested time step (adjusted as SetupTimeFreqGrid does) */
+  double TransientLength;  /* transient length */
+  int32_t TransientRemoval;/* bool: Galerkin transient removal */
+  int32_t DiscFlg;         /* bool: A <- A - beta*I */
+  double beta;             /* discount */
+  int32_t precision;       /* rsvdt_precision */
+  int32_t Display;         /* 0 silent, 1 phases, 2 progress (stdout) */
+} rsvdt_params;
+
+/* Derived time grid (SourceCode/SetupTimeFreqGrid.c:16-21). */
+typedef struct {
+  double w;        /* effective base frequency */
+  double dt;       /* adjusted time step */
+  int64_t Ns;      /* steps per period */
+  int64_t Nt;      /* transient steps */
+  int64_t ResRatio;/* Ns / Nw */
+  int64_t Nw_eff;  /* effective frequencies (Nw, or Nw/2 for a real operator) */
+  int64_t N, Nb, Nc;
+} rsvdt_grid;
+
+typedef struct rsvdt_ctx rsvdt_ctx;
+
+/* Fills defaults of SourceCode/ReadUserInput.c (k=3, q=0, Display=2, ...). */
+void rsvdt_default_params(rsvdt_params *p);
+
+/* Validates params, selects the CUDA device, creates the stream.
+ * Replaces SourceCode/PreProcessing.c:27-36 (ReadUserInput's checks and
+ * SetupTimeFreqGrid); the grid is final once the operator is set. */
+rsvdt_status rsvdt_create(const rsvdt_params *p, rsvdt_ctx **out);
+void rsvdt_destroy(rsvdt_ctx *ctx);
+const char *rsvdt_last_error(const rsvdt_ctx *ctx);
+
+/* Operator A (N x N), copied to the device together with its explicit
+ * conjugate transpose for the adjoint. Detects a real operator
+ * (||Im A||_F < 1e-12) and applies discounting.
+ * Replaces SourceCode/LNSStructure.c:22-56 (after MatLoad) and
+ * SourceCode/CreateDFTiDFTMats.c:5-97. */
+rsvdt_status rsvdt_set_operator(rsvdt_ctx *ctx, int64_t N, const int64_t *rowptr,
+                                const int64_t *col, const double *val);
+
+/* Block-CSR operator with dense bs x bs blocks (row-major inside a block);
+ * nb = N/bs block rows. Same semantics as rsvdt_set_operator. */
+rsvdt_status rsvdt_set_operator_bcsr(rsvdt_ctx *ctx, int64_t nb, int32_t bs,
+                                     const int64_t *browptr, const int64_t *bcol,
+                                     const double *val);
+
+/* Weight / input / output matrix as CSR (rows x cols). A matrix whose
+ * nonzeros are exactly its diagonal takes a fused diagonal path.
+ * Replaces SourceCode/ReadWeightMats.c:26-99 (after MatLoad). */
+rsvdt_status rsvdt_set_weight(rsvdt_ctx *ctx, rsvdt_weight which, int64_t rows, int64_t cols,
+                              const int64_t *rowptr, const int64_t *col, const double *val);
+
+/* Grid after rsvdt_set_operator. */
+rsvdt_status rsvdt_get_grid(const rsvdt_ctx *ctx, rsvdt_grid *g);
+
+/* Sketch F_hat (Nb x ncols, frequency-major) copied into the working block
+ * Y_hat; k becomes ncols / Nw_eff as in SourceCode/CreateRandomMat.c:28-30
+ * (ncols must be a multiple of Nw_eff). Replaces
+ * SourceCode/CreateRandomMat.c:23-31 (InputForcingDir). */
+rsvdt_status rsvdt_set_sketch(rsvdt_ctx *ctx, const double *F, int64_t ld, int64_t ncols);
+
+/* Random sketch: i.i.d. standard complex normal entries from a counter-based
+ * generator seeded by `seed` (SourceCode/CreateRandomMat.c:33-39, which
+ * draws from PETSc's generator instead). */
+rsvdt_status rsvdt_random_sketch(rsvdt_ctx *ctx, uint64_t seed);
+
+/* Copies the working block Y_hat (rows x k*Nw_eff) to the host; rows is Nb
+ * or Nc depending on the last action. */
+rsvdt_status rsvdt_get_block(rsvdt_ctx *ctx, double *Y, int64_t ld, int64_t *rows);
+
+/* Direct (R) or adjoint (R^H) resolvent action on the working block,
+ * weights included. Replaces SourceCode/DirectActionRK4.c:7-32 and
+ * SourceCode/AdjointActionRK4.c:7-32 with everything below them
+ * (TSActionRK4, TSRK4, CreateForcingOnFly, SaveSnapshots, DFT,
+ * TransientRemovalStrategy, ApplyWeightMats). */
+rsvdt_status rsvdt_action(rsvdt_ctx *ctx, rsvdt_dir dir);
+
+/* Orthonormalises each frequency's rows x k block in place (batched
+ * CholQR2). Replaces SourceCode/QRAllFreqs.c:5-46. */
+rsvdt_status rsvdt_qr_all_freqs(rsvdt_ctx *ctx);
+
+/* Per-frequency thin SVD of the working block. before_adjoint = 1: the
+ * block becomes its left singular vectors and is stored as U
+ * (SourceCode/SVDAllFreqsBeforeAdjoint.c:5-68 + SourceCode/StoreU.c:5-19).
+ * before_adjoint = 0: left singular vectors become V, singular values the
+ * gains, and the inverse weights are applied to U and V
+ * (SourceCode/SVDAllFreqs.c:5-79). */
+rsvdt_status rsvdt_svd_all_freqs(rsvdt_ctx *ctx, int32_t before_adjoint);
+
+/* Power iteration loop (SourceCode/PowerIterationRK4.c:8-36). */
+rsvdt_status rsvdt_power_iteration(rsvdt_ctx *ctx);
+
+/* The whole RSVD-Delta-t sequence of SourceCode/main.c:134-144 on the
+ * current sketch. */
+rsvdt_status rsvdt_run(rsvdt_ctx *ctx);
+
+/* Results of rsvdt_run: U (Nc x k*Nw_eff), V (Nb x k*Nw_eff) in the
+ * frequency-major layout, S (k x Nw_eff, column-major) gains. Any pointer
+ * may be NULL. Replaces reading Res_mat in SourceCode/SaveResults.c:32-85. */
+rsvdt_status rsvdt_get_results(rsvdt_ctx *ctx, double *U, int64_t ldu, double *V, int64_t ldv,
+                               double *S);
+
+/* Advances the RK4 state of every test vector by nsteps forced steps
+ * starting at step index i0 (1-based, as SourceCode/TSRK4.c's i), with the
+ * forcing built from the working block. Host state y (N x k, column-major,
+ * complex) and F3 (forcing at the start of step i0, N x k) are read and
+ * updated. For kernel-level tests and benchmarks; rsvdt_action is the
+ * normal entry. Replaces SourceCode/TSRK4.c:6-51 called in the loop of
+ * SourceCode/TSActionRK4.c:116-122. */
+rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps, double *y,
+                             double *F3);
+
+/* Device-resident variant of rsvdt_rk4_steps for timing: the state stays
+ * on the device between calls (reset by rsvdt_rk4_reset), nothing is
+ * copied. */
+rsvdt_status rsvdt_rk4_reset(rsvdt_ctx *ctx, rsvdt_dir dir);
+rsvdt_status rsvdt_rk4_advance(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps);
+
+/* Waits for the context's stream. */
+rsvdt_status rsvdt_synchronize(rsvdt_ctx *ctx);
+
+/* The context's cudaStream_t, for timing with events on the launching
+ * stream. */
+void *rsvdt_stream(rsvdt_ctx *ctx);
+
+/* Number of kernels the context has launched so far. */
+int64_t rsvdt_launch_count(const rsvdt_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,225 @@
+"""Oracle for the RSVD-Delta-t time-stepping path (TEST INFRASTRUCTURE).
+
+Only tests, the smoke check and the benchmark's CPU-baseline leg import
+this package, as the checker. It holds:
+  - a ctypes binding of the C restatement of the reference algorithm
+    (rsvdt_oracle.c, built into oracle/_build/liboracle.so);
+  - the dense FP64 resolvent oracle: SVD of W_q^{1/2} C (i w I - A)^{-1} B
+    W_f^{-1/2} per frequency, for problems small enough to invert.
+
+Parity status: the reference needs PETSc 3.19 + SLEPc 3.19 + MPI, none of
+which exist here or on the GPU machine, so the reference itself cannot be run.
+The restatement is pinned instead to the reference's own known answer, the
+Ginzburg-Landau tutorial (Tutorial/Ginzburg-Landau/A_GL with the parameters
+of variables.yaml:16-39 and the gains of gains.png), through the fixtures
+and script in tests/golden/.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD_DIR, "liboracle.so")
+SRC = os.path.join(HERE, "rsvdt_oracle.c")
+
+
+def build(force: bool = False) -> str:
+    """gcc -O2 -fopenmp -ffp-contract=off rsvdt_oracle.c -> _build/liboracle.so."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
+            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "rsvdt_oracle.h"))):
+        cmd = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+               SRC, "-o", LIB, "-lm"]
+        res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + res.stdout)
+    return LIB
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        P = C.POINTER
+        d = P(C.c_double)
+        i64 = C.c_int64
+        L.orc_setup_grid.argtypes = [C.c_double, i64, C.c_double, C.c_double, d, P(i64)]
+        L.orc_build_idft.argtypes = [i64, i64, C.c_int, d]
+        L.orc_build_dft.argtypes = [i64, i64, C.c_int, d]
+        L.orc_create.restype = C.c_void_p
+        L.orc_create.argtypes = [i64, P(i64), P(i64), d, i64, C.c_double, C.c_double, i64, i64, i64,
+                                 C.c_int, C.c_int]
+        L.orc_destroy.argtypes = [C.c_void_p]
+        L.orc_set_threads.argtypes = [C.c_void_p, C.c_int]
+        L.orc_set_weight.argtypes = [C.c_void_p, C.c_int, i64, i64, P(i64), P(i64), d]
+        L.orc_ts_action.argtypes = [C.c_void_p, C.c_int, i64, d, d]
+        L.orc_action.argtypes = [C.c_void_p, C.c_int, i64, d, d]
+        L.orc_rk4_steps.argtypes = [C.c_void_p, C.c_int, d, i64, i64, d, d]
+        L.orc_qr_all_freqs.argtypes = [i64, i64, i64, d]
+        L.orc_svd_all_freqs.argtypes = [i64, i64, i64, d, d, d]
+        L.orc_run.argtypes = [C.c_void_p, i64, i64, d, d, d, d]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _i(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+def setup_grid(w: float, Nw: int, dt: float, transient_length: float):
+    """(dt, Ns, Nt, ResRatio) of SourceCode/SetupTimeFreqGrid.c:16-21."""
+    out_dt = np.zeros(1)
+    ints = np.zeros(3, dtype=np.int64)
+    lib().orc_setup_grid(w, Nw, dt, transient_length, _d(out_dt), _i(ints))
+    return float(out_dt[0]), int(ints[0]), int(ints[1]), int(ints[2])
+
+
+class Oracle:
+    """CPU restatement of one resolvent problem (same entry points as the
+    CUDA library's Context)."""
+
+    def __init__(self, A, Nw: int, w: float, dt: float, transient_length: float,
+                 transient_removal: bool = False, real_op: bool | None = None, threads: int = 0):
+        A = A.tocsr()
+        A.sort_indices()
+        self.N = A.shape[0]
+        if real_op is None:
+            real_op = bool(np.linalg.norm(A.data.imag) < 1e-12)
+        self.real_op = real_op
+        self.Nw = Nw
+        self.Nw_eff = Nw // 2 if real_op else Nw
+        self.w = w
+        self.dt, self.Ns, self.Nt, self.R = setup_grid(w, Nw, dt, transient_length)
+        rp = np.ascontiguousarray(A.indptr, dtype=np.int64)
+        ci = np.ascontiguousarray(A.indices, dtype=np.int64)
+        va = np.ascontiguousarray(A.data, dtype=np.complex128)
+        self._h = lib().orc_create(self.N, _i(rp), _i(ci), _d(va.view(np.float64)), Nw, w, self.dt,
+                                   self.Ns, self.Nt, self.R, int(transient_removal), int(real_op))
+        if not self._h:
+            raise RuntimeError("oracle create failed")
+        self.Nb = self.N
+        self.Nc = self.N
+        if threads:
+            lib().orc_set_threads(self._h, threads)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().orc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_threads(self, n: int):
+        lib().orc_set_threads(self._h, n)
+
+    def set_weight(self, which: int, M):
+        M = M.tocsr()
+        M.sort_indices()
+        rp = np.ascontiguousarray(M.indptr, dtype=np.int64)
+        ci = np.ascontiguousarray(M.indices, dtype=np.int64)
+        va = np.ascontiguousarray(M.data, dtype=np.complex128)
+        rc = lib().orc_set_weight(self._h, which, M.shape[0], M.shape[1], _i(rp), _i(ci),
+                                  _d(va.view(np.float64)))
+        if rc:
+            raise RuntimeError("oracle set_weight failed")
+        if which == 1:
+            self.Nb = M.shape[1]
+        if which == 2:
+            self.Nc = M.shape[0]
+
+    def ts_action(self, direction: int, F: np.ndarray) -> np.ndarray:
+        F = np.asfortranarray(F, dtype=np.complex128)
+        k = F.shape[1] // self.Nw_eff
+        Y = np.zeros((self.N, F.shape[1]), dtype=np.complex128, order="F")
+        if lib().orc_ts_action(self._h, direction, k, _d(F), _d(Y)):
+            raise RuntimeError("oracle action failed")
+        return Y
+
+    def action(self, direction: int, Y: np.ndarray) -> np.ndarray:
+        Y = np.asfortranarray(Y, dtype=np.complex128)
+        k = Y.shape[1] // self.Nw_eff
+        rows_out = self.Nc if direction else self.Nb
+        out = np.zeros((rows_out, Y.shape[1]), dtype=np.complex128, order="F")
+        if lib().orc_action(self._h, direction, k, _d(Y), _d(out)):
+            raise RuntimeError("oracle action failed")
+        return out
+
+    def rk4_steps(self, direction: int, Fk: np.ndarray, i0: int, nsteps: int, y: np.ndarray,
+                  F3: np.ndarray):
+        Fk = np.asfortranarray(Fk, dtype=np.complex128)
+        y = np.array(y, dtype=np.complex128)
+        F3 = np.array(F3, dtype=np.complex128)
+        lib().orc_rk4_steps(self._h, direction, _d(Fk), i0, nsteps, _d(y), _d(F3))
+        return y, F3
+
+    def run(self, F: np.ndarray, q: int):
+        F = np.asfortranarray(F, dtype=np.complex128)
+        k = F.shape[1] // self.Nw_eff
+        U = np.zeros((self.Nc, F.shape[1]), dtype=np.complex128, order="F")
+        V = np.zeros((self.Nb, F.shape[1]), dtype=np.complex128, order="F")
+        S = np.zeros((k, self.Nw_eff), order="F")
+        if lib().orc_run(self._h, k, q, _d(F), _d(U), _d(V), _d(S)):
+            raise RuntimeError("oracle run failed")
+        return U, V, S
+
+
+def qr_all_freqs(Y: np.ndarray, k: int) -> np.ndarray:
+    Y = np.array(Y, dtype=np.complex128, order="F")
+    lib().orc_qr_all_freqs(Y.shape[0], k, Y.shape[1] // k, _d(Y))
+    return Y
+
+
+def svd_all_freqs(Y: np.ndarray, k: int):
+    Y = np.asfortranarray(Y, dtype=np.complex128)
+    nw = Y.shape[1] // k
+    U = np.zeros_like(Y, order="F")
+    S = np.zeros((k, nw), order="F")
+    lib().orc_svd_all_freqs(Y.shape[0], k, nw, _d(Y), _d(U), _d(S))
+    return U, S
+
+
+def freq_of(iw: int, Nw: int, w: float, real_op: bool = False) -> float:
+    """Angular frequency of column block iw: iw*w for iw < Nw/2, (iw - Nw)*w
+    otherwise (the ordering of SourceCode/CreateDFTiDFTMats.c:46-52)."""
+    if real_op or iw <= Nw // 2 - 1:
+        return iw * w
+    return (iw - Nw) * w
+
+
+def dense_resolvent_svd(A, omegas, k: int, Wq=None, Wf_inv=None, B=None, Cm=None):
+    """Dense FP64 oracle: SVD of W_q^{1/2} C (i w I - A)^{-1} B W_f^{-1/2} for
+    each w; returns (S [k, len(omegas)], U list, V list)."""
+    Ad = A.toarray() if hasattr(A, "toarray") else np.asarray(A)
+    N = Ad.shape[0]
+    S = np.zeros((k, len(omegas)))
+    Us, Vs = [], []
+    for j, om in enumerate(omegas):
+        Rm = np.linalg.solve(1j * om * np.eye(N) - Ad, np.eye(N) if B is None else B.toarray())
+        if Cm is not None:
+            Rm = Cm.toarray() @ Rm
+        if Wq is not None:
+            Rm = Wq.toarray() @ Rm
+        if Wf_inv is not None:
+            Rm = Rm @ Wf_inv.toarray()
+        u, s, vh = np.linalg.svd(Rm)
+        S[:, j] = s[:k]
+        Us.append(u[:, :k])
+        Vs.append(vh.conj().T[:, :k])
+    return S, Us, Vs

@@ -1,0 +1,858 @@
+// C ABI of the GB300 RSVD-Delta-t library (include/rsvdt.h): context,
+// operator/weight upload, the resolvent actions and the main sequence.
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+
+using namespace rsvdt;
+
+static const double kPi = 3.14159265358979323846;
+
+namespace rsvdt {
+
+bool cuda_ok(rsvdt_ctx *ctx, cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return true;
+  if (ctx) {
+    char buf[512];
+    snprintf(buf, sizeof buf, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+    ctx->err = buf;
+  }
+  return false;
+}
+
+rsvdt_status set_err(rsvdt_ctx *ctx, rsvdt_status s, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf;
+  return s;
+}
+
+void *dalloc(rsvdt_ctx *ctx, size_t bytes) {
+  void *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  ctx->allocations.push_back(p);
+  return p;
+}
+
+void dfree(rsvdt_ctx *ctx, void *p) {
+  if (!p) return;
+  for (auto &a : ctx->allocations)
+    if (a == p) {
+      cudaFree(p);
+      a = nullptr;
+      return;
+    }
+}
+
+}  // namespace rsvdt
+
+// ------------------------------------------------------------ helpers
+
+static void free_graphs(rsvdt_ctx *ctx) {
+  for (auto &g : ctx->step_graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+static bool upload(rsvdt_ctx *ctx, void *dst, const void *src, size_t bytes) {
+  return cuda_ok(ctx, cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice), "upload");
+}
+
+// Host CSR (int32) with complex values.
+struct HostCSR {
+  int64_t rows = 0, cols = 0;
+  std::vector<int32_t> rowptr, col;
+  std::vector<std::complex<double>> val;
+};
+
+static rsvdt_status csr_from_user(rsvdt_ctx *ctx, const char *name, int64_t rows, int64_t cols,
+                                  const int64_t *rowptr, const int64_t *col, const double *val,
+                                  HostCSR &m) {
+  if (rows <= 0 || cols <= 0 || !rowptr || (!col && rowptr[rows] > rowptr[0]))
+    return set_err(ctx, RSVDT_ERR_ARG, "%s: invalid CSR arguments", name);
+  const int64_t nnz = rowptr[rows] - rowptr[0];
+  if (rows >= INT32_MAX || cols >= INT32_MAX || nnz >= INT32_MAX || nnz < 0)
+    return set_err(ctx, RSVDT_ERR_ARG, "%s: sizes exceed the 32-bit device index range", name);
+  m.rows = rows;
+  m.cols = cols;
+  m.rowptr.resize(rows + 1);
+  m.col.resize(nnz);
+  m.val.resize(nnz);
+  for (int64_t i = 0; i <= rows; ++i) {
+    m.rowptr[i] = (int32_t)(rowptr[i] - rowptr[0]);
+    if (i > 0 && m.rowptr[i] < m.rowptr[i - 1])
+      return set_err(ctx, RSVDT_ERR_ARG, "%s: row pointers decrease at row %lld", name, (long long)i);
+  }
+  for (int64_t j = 0; j < nnz; ++j) {
+    const int64_t c = col[rowptr[0] + j];
+    if (c < 0 || c >= cols)
+      return set_err(ctx, RSVDT_ERR_ARG, "%s: column index %lld out of range [0, %lld)", name,
+                     (long long)c, (long long)cols);
+    m.col[j] = (int32_t)c;
+    m.val[j] = {val[2 * (rowptr[0] + j)], val[2 * (rowptr[0] + j) + 1]};
+  }
+  return RSVDT_OK;
+}
+
+// Conjugate transpose; rows of the result list the original rows in
+// ascending order (the accumulation order of SeqAIJ
+// MatMultHermitianTransposeAdd).
+static HostCSR conj_transpose(const HostCSR &a) {
+  HostCSR t;
+  t.rows = a.cols;
+  t.cols = a.rows;
+  const int64_t nnz = (int64_t)a.col.size();
+  t.rowptr.assign(t.rows + 1, 0);
+  t.col.resize(nnz);
+  t.val.resize(nnz);
+  for (int64_t j = 0; j < nnz; ++j) t.rowptr[a.col[j] + 1]++;
+  for (int64_t i = 0; i < t.rows; ++i) t.rowptr[i + 1] += t.rowptr[i];
+  std::vector<int32_t> fill(t.rowptr.begin(), t.rowptr.end() - 1);
+  for (int64_t i = 0; i < a.rows; ++i)
+    for (int32_t j = a.rowptr[i]; j < a.rowptr[i + 1]; ++j) {
+      const int32_t c = a.col[j];
+      t.col[fill[c]] = (int32_t)i;
+      t.val[fill[c]] = std::conj(a.val[j]);
+      fill[c]++;
+    }
+  return t;
+}
+
+static rsvdt_status upload_csr(rsvdt_ctx *ctx, const HostCSR &h, DevCSR &d, bool with32) {
+  d.rows = h.rows;
+  d.cols = h.cols;
+  d.nnz = (int64_t)h.col.size();
+  d.rowptr = (int32_t *)dalloc(ctx, sizeof(int32_t) * (h.rows + 1));
+  d.col = (int32_t *)dalloc(ctx, sizeof(int32_t) * (d.nnz ? d.nnz : 1));
+  d.val = (z128 *)dalloc(ctx, sizeof(z128) * (d.nnz ? d.nnz : 1));
+  if (!d.rowptr || !d.col || !d.val) return set_err(ctx, RSVDT_ERR_OOM, "device allocation for a sparse matrix failed");
+  if (!upload(ctx, d.rowptr, h.rowptr.data(), sizeof(int32_t) * (h.rows + 1)) ||
+      (d.nnz && !upload(ctx, d.col, h.col.data(), sizeof(int32_t) * d.nnz)) ||
+      (d.nnz && !upload(ctx, d.val, h.val.data(), sizeof(z128) * d.nnz)))
+    return RSVDT_ERR_CUDA;
+  if (with32) {
+    std::vector<z64> v32(d.nnz);
+    for (int64_t j = 0; j < d.nnz; ++j) v32[j] = zmake<z64>((float)h.val[j].real(), (float)h.val[j].imag());
+    d.val32 = (z64 *)dalloc(ctx, sizeof(z64) * (d.nnz ? d.nnz : 1));
+    if (!d.val32) return set_err(ctx, RSVDT_ERR_OOM, "device allocation for a sparse matrix failed");
+    if (d.nnz && !upload(ctx, d.val32, v32.data(), sizeof(z64) * d.nnz)) return RSVDT_ERR_CUDA;
+  }
+  bool diag = h.rows == h.cols;
+  for (int64_t i = 0; i < h.rows && diag; ++i)
+    diag = (h.rowptr[i + 1] - h.rowptr[i] == 1) && h.col[h.rowptr[i]] == i;
+  d.diag = diag;
+  d.present = true;
+  return RSVDT_OK;
+}
+
+static void free_csr(rsvdt_ctx *ctx, DevCSR &d) {
+  dfree(ctx, d.rowptr);
+  dfree(ctx, d.col);
+  dfree(ctx, d.val);
+  dfree(ctx, d.val32);
+  d = DevCSR();
+}
+
+static void free_bcsr(rsvdt_ctx *ctx, DevBCSR &d) {
+  dfree(ctx, d.browptr);
+  dfree(ctx, d.bcol);
+  dfree(ctx, d.val);
+  dfree(ctx, d.val32);
+  d = DevBCSR();
+}
+
+// SetupTimeFreqGrid (SourceCode/SetupTimeFreqGrid.c:16-21) and the DFT /
+// iDFT tables (SourceCode/CreateDFTiDFTMats.c:18-93), computed on the host
+// exactly as the reference forms them and stored for the device:
+// tab[jt][iw] = idft[iw][jt], dft[iw][p].
+static rsvdt_status setup_grid_and_tables(rsvdt_ctx *ctx) {
+  const rsvdt_params &p = ctx->par;
+  ctx->w = p.w * (p.TwoPI ? 2 * kPi : 1);  // SourceCode/ReadUserInput.c:82
+  const double T = 2 * kPi / ctx->w;
+  const double dt_w = T / (double)p.Nw;
+  ctx->dt = dt_w / std::ceil(dt_w / p.dt);
+  ctx->Ns = (int64_t)std::llround(T / ctx->dt);
+  ctx->Nt = (int64_t)std::llround(p.TransientLength / ctx->dt);
+  ctx->Nw = p.Nw;
+  ctx->R = ctx->Ns / p.Nw;
+  ctx->Nw_eff = ctx->real_op ? p.Nw / 2 : p.Nw;  // SourceCode/LNSStructure.c:44
+  if (ctx->R < 1 || ctx->Nw_eff < 1)
+    return set_err(ctx, RSVDT_ERR_ARG, "time grid is degenerate (Ns=%lld, Nw=%lld)", (long long)ctx->Ns,
+                   (long long)p.Nw);
+  const int64_t Nwe = ctx->Nw_eff, Nt2 = 2 * ctx->Ns, Nw = ctx->Nw;
+  std::vector<z128> tab((size_t)Nt2 * Nwe);
+  std::vector<z64> tab32((size_t)Nt2 * Nwe);
+  const double alpha_im = -2 * kPi / (double)Nt2;
+  for (int64_t iw = 0; iw < Nwe; ++iw) {
+    int64_t f;
+    if (ctx->real_op)
+      f = iw;
+    else if (Nwe % 2 == 0)
+      f = (iw <= Nwe / 2 - 1) ? iw : (iw - Nwe) + Nt2;
+    else
+      f = (iw <= (Nwe - 1) / 2) ? iw : (iw - Nwe) + Nt2;
+    const double v_im = alpha_im * (double)f;
+    for (int64_t it = 0; it < Nt2; ++it) {
+      const double y = v_im * (double)it;
+      const double s = 2. / (double)Nt2;
+      const z128 e = zmake<z128>(std::cos(y) * s, -std::sin(y) * s);
+      tab[(size_t)(it * Nwe + iw)] = e;
+      tab32[(size_t)(it * Nwe + iw)] = zmake<z64>((float)e.re, (float)e.im);
+    }
+  }
+  std::vector<z128> dft((size_t)Nwe * Nw);
+  const double a_dft = ctx->real_op ? -2 * kPi / (double)(2 * Nw) : -2 * kPi / (double)Nw;
+  for (int64_t iw = 0; iw < Nwe; ++iw) {
+    const double v_im = a_dft * (double)iw;
+    for (int64_t j = 0; j < Nw; ++j) {
+      const double y = v_im * (double)j;
+      dft[(size_t)(iw * Nw + j)] = zmake<z128>(std::cos(y), std::sin(y));
+    }
+  }
+  dfree(ctx, ctx->tab);
+  dfree(ctx, ctx->tab32);
+  dfree(ctx, ctx->dft);
+  ctx->tab = (z128 *)dalloc(ctx, sizeof(z128) * tab.size());
+  ctx->tab32 = (z64 *)dalloc(ctx, sizeof(z64) * tab32.size());
+  ctx->dft = (z128 *)dalloc(ctx, sizeof(z128) * dft.size());
+  if (!ctx->tab || !ctx->tab32 || !ctx->dft) return set_err(ctx, RSVDT_ERR_OOM, "table allocation failed");
+  if (!upload(ctx, ctx->tab, tab.data(), sizeof(z128) * tab.size()) ||
+      !upload(ctx, ctx->tab32, tab32.data(), sizeof(z64) * tab32.size()) ||
+      !upload(ctx, ctx->dft, dft.data(), sizeof(z128) * dft.size()))
+    return RSVDT_ERR_CUDA;
+  free_graphs(ctx);
+  return RSVDT_OK;
+}
+
+// Device buffers for K test vectors.
+static rsvdt_status ensure_buffers(rsvdt_ctx *ctx, int64_t K) {
+  const int64_t N = ctx->N, Nwe = ctx->Nw_eff;
+  const int64_t rows = std::max(N, std::max(ctx->Nb, ctx->Nc));
+  const size_t blk_elems = (size_t)rows * Nwe * K;
+  const int64_t Nstore = ctx->Nw + 1;  // room for the transient-removal sample
+  if (ctx->K == K && ctx->y && ctx->blk_elems >= blk_elems) return RSVDT_OK;
+  free_graphs(ctx);
+  void **bufs[] = {&ctx->y, &ctx->zA, &ctx->zB, &ctx->acc, &ctx->F2, &ctx->F3};
+  for (auto b : bufs) {
+    dfree(ctx, *b);
+    *b = dalloc(ctx, sizeof(z128) * N * K);
+    if (!*b) return set_err(ctx, RSVDT_ERR_OOM, "state allocation failed");
+  }
+  dfree(ctx, ctx->ring);
+  ctx->ring = dalloc(ctx, sizeof(z128) * Nstore * N * K);
+  dfree(ctx, ctx->Fh);
+  ctx->Fh = dalloc(ctx, sizeof(z128) * N * Nwe * K);
+  // Keep the working block's contents when it is only re-sized upward.
+  z128 *old = ctx->blk;
+  size_t old_elems = ctx->blk_elems;
+  z128 *nb = (z128 *)dalloc(ctx, sizeof(z128) * blk_elems);
+  if (nb && old) cudaMemcpy(nb, old, sizeof(z128) * std::min(old_elems, blk_elems), cudaMemcpyDeviceToDevice);
+  dfree(ctx, old);
+  ctx->blk = nb;
+  dfree(ctx, ctx->blk2);
+  ctx->blk2 = (z128 *)dalloc(ctx, sizeof(z128) * blk_elems);
+  dfree(ctx, ctx->S);
+  ctx->S = (double *)dalloc(ctx, sizeof(double) * Nwe * K);
+  if (!ctx->ring || !ctx->Fh || !ctx->blk || !ctx->blk2 || !ctx->S)
+    return set_err(ctx, RSVDT_ERR_OOM, "spectral block allocation failed (%zu complex values each)", blk_elems);
+  ctx->blk_elems = blk_elems;
+  ctx->K = K;
+  return RSVDT_OK;
+}
+
+// Nb / Nc from the weights known so far (SourceCode/ReadWeightMats.c:50-52,
+// 90, 95); no cross-checks.
+static void update_dims(rsvdt_ctx *ctx) {
+  ctx->Nb = ctx->W[RSVDT_B].present ? ctx->W[RSVDT_B].cols : ctx->N;
+  ctx->Nc = ctx->W[RSVDT_C].present ? ctx->W[RSVDT_C].rows : ctx->N;
+}
+
+static rsvdt_status check_weights(rsvdt_ctx *ctx) {
+  // SourceCode/ReadWeightMats.c:26-99 size rules.
+  const int64_t N = ctx->N;
+  DevCSR *W = ctx->W;
+  int64_t nb = W[RSVDT_B].present ? W[RSVDT_B].cols : N;
+  int64_t nc = W[RSVDT_C].present ? W[RSVDT_C].rows : N;
+  if (W[RSVDT_B].present && W[RSVDT_B].rows != N)
+    return set_err(ctx, RSVDT_ERR_ARG, "Input matrix (B) must have %lld rows, current size = %lld x %lld",
+                   (long long)N, (long long)W[RSVDT_B].rows, (long long)W[RSVDT_B].cols);
+  if (W[RSVDT_W_F_SQRT_INV].present && W[RSVDT_W_F_SQRT_INV].cols != nb)
+    return set_err(ctx, RSVDT_ERR_ARG,
+                   "Size mismatch between input matrix (B) and input weight matrix (W_f_sqrt_inv), %lld != %lld",
+                   (long long)nb, (long long)W[RSVDT_W_F_SQRT_INV].cols);
+  if (W[RSVDT_C].present && W[RSVDT_C].cols != N)
+    return set_err(ctx, RSVDT_ERR_ARG, "Output matrix (C) must have %lld columns, current size = %lld x %lld",
+                   (long long)N, (long long)W[RSVDT_C].rows, (long long)W[RSVDT_C].cols);
+  if (W[RSVDT_W_Q_SQRT].present && W[RSVDT_W_Q_SQRT].rows != nc)
+    return set_err(ctx, RSVDT_ERR_ARG,
+                   "Size mismatch between output matrix (C) and output weight matrix (W_q_sqrt), %lld != %lld",
+                   (long long)nc, (long long)W[RSVDT_W_Q_SQRT].rows);
+  if (W[RSVDT_W_Q_SQRT_INV].present && W[RSVDT_W_Q_SQRT_INV].rows != nc)
+    return set_err(ctx, RSVDT_ERR_ARG,
+                   "Size mismatch between output matrix (C) and inverse output weight matrix (W_q_sqrt_inv), %lld != %lld",
+                   (long long)nc, (long long)W[RSVDT_W_Q_SQRT_INV].rows);
+  ctx->Nb = nb;
+  ctx->Nc = nc;
+  return RSVDT_OK;
+}
+
+#define RSVDT_TRY(x)                   \
+  do {                                 \
+    rsvdt_status _s = (x);             \
+    if (_s != RSVDT_OK) return _s;     \
+  } while (0)
+
+// Y <- M Y on the working block (ping-pong between blk and blk2).
+static rsvdt_status weight_step(rsvdt_ctx *ctx, const DevCSR &M, int64_t rows_in) {
+  if (!M.present) return RSVDT_OK;
+  if (M.cols != rows_in)
+    return set_err(ctx, RSVDT_ERR_ARG, "weight product: %lld columns but the block has %lld rows",
+                   (long long)M.cols, (long long)rows_in);
+  RSVDT_TRY(apply_weight(ctx, M, ctx->blk, ctx->blk2, ctx->Nw_eff * ctx->K));
+  std::swap(ctx->blk, ctx->blk2);
+  ctx->blk_rows = M.rows;
+  return RSVDT_OK;
+}
+
+// Copies the working block (N rows) into the forcing-coefficient buffer in
+// the action's precision (TSActionRK4 copies Y_hat to F_hat,
+// SourceCode/TSActionRK4.c:49).
+static rsvdt_status stage_forcing(rsvdt_ctx *ctx, int prec) {
+  const int64_t n = ctx->N * ctx->Nw_eff * ctx->K;
+  if (prec == RSVDT_PREC_C64) return launch_convert_to64(ctx, ctx->blk, (z64 *)ctx->Fh, n);
+  return cuda_ok(ctx, cudaMemcpyAsync(ctx->Fh, ctx->blk, sizeof(z128) * n, cudaMemcpyDeviceToDevice, ctx->stream),
+                 "copy")
+             ? RSVDT_OK
+             : RSVDT_ERR_CUDA;
+}
+
+static rsvdt_status require_ready(rsvdt_ctx *ctx, bool need_block) {
+  if (!ctx) return RSVDT_ERR_ARG;
+  if (!ctx->have_operator) return set_err(ctx, RSVDT_ERR_STATE, "the operator has not been set");
+  if (need_block && !ctx->have_block) return set_err(ctx, RSVDT_ERR_STATE, "no sketch / working block");
+  return RSVDT_OK;
+}
+
+// ---------------------------------------------------------------- ABI
+
+extern "C" {
+
+void rsvdt_default_params(rsvdt_params *p) {
+  std::memset(p, 0, sizeof(*p));
+  p->k = 3;  // SourceCode/ReadUserInput.c:109-113
+  p->q = 0;  // :114-118
+  p->Nw = 0;
+  p->w = 0;
+  p->TwoPI = 0;
+  p->dt = 0;
+  p->TransientLength = 0;
+  p->TransientRemoval = 0;
+  p->DiscFlg = 0;
+  p->beta = 0;
+  p->precision = RSVDT_PREC_C128;
+  p->Display = 2;  // :126-130
+}
+
+rsvdt_status rsvdt_create(const rsvdt_params *p, rsvdt_ctx **out) {
+  if (!p || !out) return RSVDT_ERR_ARG;
+  *out = nullptr;
+  rsvdt_ctx *ctx = new rsvdt_ctx();
+  ctx->par = *p;
+  rsvdt_status st = RSVDT_OK;
+  if (p->k < 1) st = set_err(ctx, RSVDT_ERR_ARG, "'k' must be positive, current value: %lld", (long long)p->k);
+  else if (p->q < 0) st = set_err(ctx, RSVDT_ERR_ARG, "'q' must be non-negative, current value: %lld", (long long)p->q);
+  else if (p->Nw < 1) st = set_err(ctx, RSVDT_ERR_ARG, "Must specify 'Nw'");
+  else if (!(p->w > 0)) st = set_err(ctx, RSVDT_ERR_ARG, "Must specify 'w' (a positive base frequency)");
+  else if (!(p->dt > 0)) st = set_err(ctx, RSVDT_ERR_ARG, "Must specify 'dt' (a positive time step)");
+  else if (!(p->TransientLength >= 0)) st = set_err(ctx, RSVDT_ERR_ARG, "Must specify 'TransientLength'");
+  else if (p->DiscFlg && p->beta < 0)
+    st = set_err(ctx, RSVDT_ERR_ARG, "'beta' must be positive, current value: %g", p->beta);
+  else if (p->precision != RSVDT_PREC_C128 && p->precision != RSVDT_PREC_C64)
+    st = set_err(ctx, RSVDT_ERR_ARG, "unknown precision %d", (int)p->precision);
+  if (st == RSVDT_OK) {
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev < 1) {
+      cudaGetLastError();
+      st = set_err(ctx, RSVDT_ERR_CUDA, "no CUDA device available (%s)", cudaGetErrorString(e));
+    }
+  }
+  if (st == RSVDT_OK) {
+    cudaGetDevice(&ctx->device);
+    if (!cuda_ok(ctx, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "stream create"))
+      st = RSVDT_ERR_CUDA;
+  }
+  if (st == RSVDT_OK) {
+    ctx->d_step = (int64_t *)dalloc(ctx, sizeof(int64_t) * 2);
+    ctx->d_flags = (int32_t *)dalloc(ctx, sizeof(int32_t) * 4);
+    if (!ctx->d_step || !ctx->d_flags) st = set_err(ctx, RSVDT_ERR_OOM, "device allocation failed");
+  }
+  if (st != RSVDT_OK) {
+    // Keep the context so that rsvdt_last_error can report; the caller
+    // destroys it.
+    *out = ctx;
+    return st;
+  }
+  ctx->K = 0;
+  *out = ctx;
+  return RSVDT_OK;
+}
+
+void rsvdt_destroy(rsvdt_ctx *ctx) {
+  if (!ctx) return;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  free_graphs(ctx);
+  for (void *p : ctx->allocations)
+    if (p) cudaFree(p);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char *rsvdt_last_error(const rsvdt_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+rsvdt_status rsvdt_set_operator(rsvdt_ctx *ctx, int64_t N, const int64_t *rowptr, const int64_t *col,
+                                const double *val) {
+  if (!ctx) return RSVDT_ERR_ARG;
+  HostCSR A;
+  RSVDT_TRY(csr_from_user(ctx, "operator A", N, N, rowptr, col, val, A));
+  // Real-valued check (SourceCode/LNSStructure.c:37-44).
+  double im2 = 0;
+  for (auto &v : A.val) im2 += v.imag() * v.imag();
+  ctx->real_op = std::sqrt(im2) < 1e-12;
+  // Discounting A <- A - beta I (SourceCode/LNSStructure.c:53-56); MatShift
+  // inserts missing diagonal entries.
+  if (ctx->par.DiscFlg) {
+    HostCSR B;
+    B.rows = B.cols = N;
+    B.rowptr.push_back(0);
+    for (int64_t i = 0; i < N; ++i) {
+      bool found = false;
+      for (int32_t j = A.rowptr[i]; j < A.rowptr[i + 1]; ++j) {
+        if (!found && A.col[j] > i) {
+          B.col.push_back((int32_t)i);
+          B.val.push_back(-ctx->par.beta);
+          found = true;
+        }
+        std::complex<double> v = A.val[j];
+        if (A.col[j] == i) {
+          v -= ctx->par.beta;
+          found = true;
+        }
+        B.col.push_back(A.col[j]);
+        B.val.push_back(v);
+      }
+      if (!found) {
+        B.col.push_back((int32_t)i);
+        B.val.push_back(-ctx->par.beta);
+      }
+      B.rowptr.push_back((int32_t)B.col.size());
+    }
+    A = std::move(B);
+  }
+  HostCSR AH = conj_transpose(A);
+  free_csr(ctx, ctx->A);
+  free_csr(ctx, ctx->AH);
+  free_bcsr(ctx, ctx->BA);
+  free_bcsr(ctx, ctx->BAH);
+  RSVDT_TRY(upload_csr(ctx, A, ctx->A, true));
+  RSVDT_TRY(upload_csr(ctx, AH, ctx->AH, true));
+  ctx->N = N;
+  ctx->have_operator = true;
+  update_dims(ctx);
+  RSVDT_TRY(setup_grid_and_tables(ctx));
+  return ensure_buffers(ctx, ctx->K > 0 ? ctx->K : ctx->par.k);
+}
+
+rsvdt_status rsvdt_set_operator_bcsr(rsvdt_ctx *ctx, int64_t nb, int32_t bs, const int64_t *browptr,
+                                     const int64_t *bcol, const double *val) {
+  if (!ctx) return RSVDT_ERR_ARG;
+  if (nb <= 0 || bs <= 0 || bs > 16 || !browptr)
+    return set_err(ctx, RSVDT_ERR_ARG, "invalid block-CSR arguments (nb=%lld, bs=%d)", (long long)nb, bs);
+  const int64_t N = nb * bs;
+  const int64_t nblk = browptr[nb] - browptr[0];
+  if (N >= INT32_MAX || nblk < 0 || nblk >= INT32_MAX)
+    return set_err(ctx, RSVDT_ERR_ARG, "block-CSR sizes exceed the 32-bit device index range");
+  const int64_t bb = (int64_t)bs * bs;
+  std::vector<int32_t> rp(nb + 1), cl(nblk);
+  std::vector<std::complex<double>> vl(nblk * bb);
+  double im2 = 0;
+  for (int64_t i = 0; i <= nb; ++i) {
+    rp[i] = (int32_t)(browptr[i] - browptr[0]);
+    if (i > 0 && rp[i] < rp[i - 1]) return set_err(ctx, RSVDT_ERR_ARG, "block row pointers decrease");
+  }
+  for (int64_t j = 0; j < nblk; ++j) {
+    const int64_t c = bcol[browptr[0] + j];
+    if (c < 0 || c >= nb) return set_err(ctx, RSVDT_ERR_ARG, "block column %lld out of range", (long long)c);
+    cl[j] = (int32_t)c;
+  }
+  for (int64_t e = 0; e < nblk * bb; ++e) {
+    vl[e] = {val[2 * (browptr[0] * bb + e)], val[2 * (browptr[0] * bb + e) + 1]};
+    im2 += vl[e].imag() * vl[e].imag();
+  }
+  ctx->real_op = std::sqrt(im2) < 1e-12;
+  if (ctx->par.DiscFlg) {
+    for (int64_t i = 0; i < nb; ++i) {
+      bool found = false;
+      for (int32_t j = rp[i]; j < rp[i + 1]; ++j)
+        if (cl[j] == i) {
+          for (int r = 0; r < bs; ++r) vl[(int64_t)j * bb + r * bs + r] -= ctx->par.beta;
+          found = true;
+        }
+      if (!found)
+        return set_err(ctx, RSVDT_ERR_ARG, "discounting needs a stored diagonal block in block row %lld",
+                       (long long)i);
+    }
+  }
+  // Conjugate transpose: block (I,J) -> (J,I) with each block conjugate-transposed.
+  std::vector<int32_t> trp(nb + 1, 0), tcl(nblk);
+  std::vector<std::complex<double>> tvl(nblk * bb);
+  for (int64_t j = 0; j < nblk; ++j) trp[cl[j] + 1]++;
+  for (int64_t i = 0; i < nb; ++i) trp[i + 1] += trp[i];
+  std::vector<int32_t> fill(trp.begin(), trp.end() - 1);
+  for (int64_t i = 0; i < nb; ++i)
+    for (int32_t j = rp[i]; j < rp[i + 1]; ++j) {
+      const int32_t d = fill[cl[j]]++;
+      tcl[d] = (int32_t)i;
+      for (int r = 0; r < bs; ++r)
+        for (int c = 0; c < bs; ++c) tvl[(int64_t)d * bb + c * bs + r] = std::conj(vl[(int64_t)j * bb + r * bs + c]);
+    }
+  free_csr(ctx, ctx->A);
+  free_csr(ctx, ctx->AH);
+  free_bcsr(ctx, ctx->BA);
+  free_bcsr(ctx, ctx->BAH);
+  auto up = [&](DevBCSR &d, const std::vector<int32_t> &r, const std::vector<int32_t> &c,
+                const std::vector<std::complex<double>> &v) -> rsvdt_status {
+    d.bs = bs;
+    d.nb = nb;
+    d.nblocks = nblk;
+    d.browptr = (int32_t *)dalloc(ctx, sizeof(int32_t) * (nb + 1));
+    d.bcol = (int32_t *)dalloc(ctx, sizeof(int32_t) * (nblk ? nblk : 1));
+    d.val = (z128 *)dalloc(ctx, sizeof(z128) * (nblk ? nblk * bb : 1));
+    d.val32 = (z64 *)dalloc(ctx, sizeof(z64) * (nblk ? nblk * bb : 1));
+    if (!d.browptr || !d.bcol || !d.val || !d.val32) return set_err(ctx, RSVDT_ERR_OOM, "block-CSR allocation failed");
+    std::vector<z64> v32(v.size());
+    for (size_t e = 0; e < v.size(); ++e) v32[e] = zmake<z64>((float)v[e].real(), (float)v[e].imag());
+    if (!upload(ctx, d.browptr, r.data(), sizeof(int32_t) * (nb + 1)) ||
+        (nblk && !upload(ctx, d.bcol, c.data(), sizeof(int32_t) * nblk)) ||
+        (nblk && !upload(ctx, d.val, v.data(), sizeof(z128) * nblk * bb)) ||
+        (nblk && !upload(ctx, d.val32, v32.data(), sizeof(z64) * nblk * bb)))
+      return RSVDT_ERR_CUDA;
+    d.present = true;
+    return RSVDT_OK;
+  };
+  RSVDT_TRY(up(ctx->BA, rp, cl, vl));
+  RSVDT_TRY(up(ctx->BAH, trp, tcl, tvl));
+  ctx->N = N;
+  ctx->have_operator = true;
+  update_dims(ctx);
+  RSVDT_TRY(setup_grid_and_tables(ctx));
+  return ensure_buffers(ctx, ctx->K > 0 ? ctx->K : ctx->par.k);
+}
+
+rsvdt_status rsvdt_set_weight(rsvdt_ctx *ctx, rsvdt_weight which, int64_t rows, int64_t cols,
+                              const int64_t *rowptr, const int64_t *col, const double *val) {
+  if (!ctx) return RSVDT_ERR_ARG;
+  if ((int)which < 0 || (int)which > 4) return set_err(ctx, RSVDT_ERR_ARG, "unknown weight %d", (int)which);
+  static const char *names[] = {"W_f_sqrt_inv", "B", "C", "W_q_sqrt", "W_q_sqrt_inv"};
+  if ((which == RSVDT_W_F_SQRT_INV || which == RSVDT_W_Q_SQRT || which == RSVDT_W_Q_SQRT_INV) && rows != cols)
+    return set_err(ctx, RSVDT_ERR_ARG, "%s must be square, current size = %lld x %lld", names[which],
+                   (long long)rows, (long long)cols);
+  HostCSR h;
+  RSVDT_TRY(csr_from_user(ctx, names[which], rows, cols, rowptr, col, val, h));
+  free_csr(ctx, ctx->W[which]);
+  free_csr(ctx, ctx->WH[which]);
+  RSVDT_TRY(upload_csr(ctx, h, ctx->W[which], false));
+  RSVDT_TRY(upload_csr(ctx, conj_transpose(h), ctx->WH[which], false));
+  // Sizes are cross-checked once all matrices are known (at the sketch and
+  // at every action), as ReadWeightMats checks them after reading them all.
+  if (ctx->have_operator) {
+    update_dims(ctx);
+    RSVDT_TRY(ensure_buffers(ctx, ctx->K > 0 ? ctx->K : ctx->par.k));
+  }
+  return RSVDT_OK;
+}
+
+rsvdt_status rsvdt_get_grid(const rsvdt_ctx *ctx, rsvdt_grid *g) {
+  if (!ctx || !g) return RSVDT_ERR_ARG;
+  if (!ctx->have_operator) return RSVDT_ERR_STATE;
+  g->w = ctx->w;
+  g->dt = ctx->dt;
+  g->Ns = ctx->Ns;
+  g->Nt = ctx->Nt;
+  g->ResRatio = ctx->R;
+  g->Nw_eff = ctx->Nw_eff;
+  g->N = ctx->N;
+  g->Nb = ctx->Nb;
+  g->Nc = ctx->Nc;
+  return RSVDT_OK;
+}
+
+rsvdt_status rsvdt_set_sketch(rsvdt_ctx *ctx, const double *F, int64_t ld, int64_t ncols) {
+  RSVDT_TRY(require_ready(ctx, false));
+  RSVDT_TRY(check_weights(ctx));
+  if (!F || ld < ctx->Nb) return set_err(ctx, RSVDT_ERR_ARG, "invalid sketch arguments");
+  if (ncols < ctx->Nw_eff || ncols % ctx->Nw_eff != 0)
+    return set_err(ctx, RSVDT_ERR_ARG, "Input forcing must have a multiple of Nw_eff = %lld columns, current size = %lld x %lld",
+                   (long long)ctx->Nw_eff, (long long)ctx->Nb, (long long)ncols);
+  RSVDT_TRY(ensure_buffers(ctx, ncols / ctx->Nw_eff));
+  const int64_t K = ctx->K, C = ctx->Nw_eff * K, rows = ctx->Nb;
+  z128 *stage = (z128 *)dalloc(ctx, sizeof(z128) * ld * C);
+  if (!stage) return set_err(ctx, RSVDT_ERR_OOM, "staging allocation failed");
+  rsvdt_status st = RSVDT_OK;
+  if (!cuda_ok(ctx, cudaMemcpyAsync(stage, F, sizeof(z128) * ld * C, cudaMemcpyHostToDevice, ctx->stream), "upload"))
+    st = RSVDT_ERR_CUDA;
+  if (!st) st = launch_colmajor_to_blk(ctx, stage, rows, ld, C, ctx->blk);
+  if (!st && !cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync")) st = RSVDT_ERR_CUDA;
+  dfree(ctx, stage);
+  if (st) return st;
+  ctx->blk_rows = rows;
+  ctx->have_block = true;
+  ctx->have_results = false;
+  return RSVDT_OK;
+}
+
+rsvdt_status rsvdt_random_sketch(rsvdt_ctx *ctx, uint64_t seed) {
+  RSVDT_TRY(require_ready(ctx, false));
+  RSVDT_TRY(launch_random(ctx, ctx->blk, ctx->Nb * ctx->Nw_eff * ctx->K, seed));
+  ctx->blk_rows = ctx->Nb;
+  ctx->have_block = true;
+  ctx->have_results = false;
+  return cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
+}
+
+rsvdt_status rsvdt_get_block(rsvdt_ctx *ctx, double *Y, int64_t ld, int64_t *rows) {
+  RSVDT_TRY(require_ready(ctx, true));
+  const int64_t C = ctx->Nw_eff * ctx->K, r = ctx->blk_rows;
+  if (rows) *rows = r;
+  if (!Y) return RSVDT_OK;
+  if (ld < r) return set_err(ctx, RSVDT_ERR_ARG, "ld (%lld) < rows (%lld)", (long long)ld, (long long)r);
+  z128 *stage = (z128 *)dalloc(ctx, sizeof(z128) * ld * C);
+  if (!stage) return set_err(ctx, RSVDT_ERR_OOM, "staging allocation failed");
+  rsvdt_status st = launch_blk_to_colmajor(ctx, ctx->blk, r, C, stage, ld);
+  if (!st && !cuda_ok(ctx, cudaMemcpyAsync(Y, stage, sizeof(z128) * ld * C, cudaMemcpyDeviceToHost, ctx->stream),
+                      "download"))
+    st = RSVDT_ERR_CUDA;
+  if (!st && !cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync")) st = RSVDT_ERR_CUDA;
+  dfree(ctx, stage);
+  return st;
+}
+
+rsvdt_status rsvdt_action(rsvdt_ctx *ctx, rsvdt_dir dir) {
+  RSVDT_TRY(require_ready(ctx, true));
+  const int d = dir == RSVDT_DIRECT ? 1 : 0;
+  const int prec = ctx->par.precision;
+  RSVDT_TRY(check_weights(ctx));
+  const int64_t rows_in = d ? ctx->Nb : ctx->Nc;
+  if (ctx->blk_rows != rows_in)
+    return set_err(ctx, RSVDT_ERR_STATE, "%s action needs a block of %lld rows, the working block has %lld",
+                   d ? "direct" : "adjoint", (long long)rows_in, (long long)ctx->blk_rows);
+  if (ctx->par.Display >= 1) printf("\n*** %s action begins! ***\n", d ? "Direct" : "Adjoint");
+  // ApplyWeightMats before (SourceCode/ApplyWeightMats.c:17-28, 43-60).
+  if (d) {
+    RSVDT_TRY(weight_step(ctx, ctx->W[RSVDT_W_F_SQRT_INV], ctx->blk_rows));
+    RSVDT_TRY(weight_step(ctx, ctx->W[RSVDT_B], ctx->blk_rows));
+  } else {
+    RSVDT_TRY(weight_step(ctx, ctx->WH[RSVDT_W_Q_SQRT], ctx->blk_rows));
+    RSVDT_TRY(weight_step(ctx, ctx->WH[RSVDT_C], ctx->blk_rows));
+  }
+  if (ctx->blk_rows != ctx->N) return set_err(ctx, RSVDT_ERR_ARG, "forcing block has %lld rows, expected N", (long long)ctx->blk_rows);
+  // TSActionRK4 (SourceCode/TSActionRK4.c:38-148).
+  const bool tr = ctx->par.TransientRemoval != 0;
+  ctx->Nstore = tr ? ctx->Nw + 1 : ctx->Nw;
+  const int64_t rend = ctx->Nt + ctx->Ns + (tr ? ctx->R : 0);
+  RSVDT_TRY(stage_forcing(ctx, prec));
+  if (!cuda_ok(ctx, cudaMemsetAsync(ctx->d_flags, 0, sizeof(int32_t) * 4, ctx->stream), "memset")) return RSVDT_ERR_CUDA;
+  RSVDT_TRY(launch_forcing_init(ctx, d, prec));
+  RSVDT_TRY(run_steps(ctx, d, prec, 1, rend, true));
+  if (tr) {
+    RSVDT_TRY(transient_removal(ctx, d, prec, ctx->blk2));
+  } else {
+    RSVDT_TRY(launch_dft(ctx, prec, ctx->blk2));
+  }
+  std::swap(ctx->blk, ctx->blk2);
+  ctx->blk_rows = ctx->N;
+  // ApplyWeightMats after (SourceCode/ApplyWeightMats.c:29-41, 61-79).
+  if (d) {
+    RSVDT_TRY(weight_step(ctx, ctx->W[RSVDT_C], ctx->blk_rows));
+    RSVDT_TRY(weight_step(ctx, ctx->W[RSVDT_W_Q_SQRT], ctx->blk_rows));
+  } else {
+    RSVDT_TRY(weight_step(ctx, ctx->WH[RSVDT_B], ctx->blk_rows));
+    RSVDT_TRY(weight_step(ctx, ctx->WH[RSVDT_W_F_SQRT_INV], ctx->blk_rows));
+  }
+  bool ok = true;
+  RSVDT_TRY(check_finite(ctx, ctx->blk, ctx->blk_rows * ctx->Nw_eff * ctx->K, &ok));
+  if (!ok) return set_err(ctx, RSVDT_ERR_DIVERGED, "NaN or Inf in the %s action's response", d ? "direct" : "adjoint");
+  if (ctx->par.Display >= 1) printf("*** %s action done ***\n", d ? "Direct" : "Adjoint");
+  return RSVDT_OK;
+}
+
+rsvdt_status rsvdt_qr_all_freqs(rsvdt_ctx *ctx) {
+  RSVDT_TRY(require_ready(ctx, true));
+  RSVDT_TRY(cholqr2(ctx, ctx->blk, ctx->blk_rows, ctx->Nw_eff, ctx->K, nullptr));
+  return cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
+}
+
+rsvdt_status rsvdt_svd_all_freqs(rsvdt_ctx *ctx, int32_t before_adjoint) {
+  RSVDT_TRY(require_ready(ctx, true));
+  const int64_t rows = ctx->blk_rows, n = rows * ctx->Nw_eff * ctx->K;
+  if (before_adjoint) {
+    RSVDT_TRY(svd_all(ctx, ctx->blk, rows, ctx->Nw_eff, ctx->K, nullptr, ctx->S));
+    // StoreU (SourceCode/StoreU.c:15).
+    dfree(ctx, ctx->Ublk);
+    ctx->Ublk = (z128 *)dalloc(ctx, sizeof(z128) * n);
+    if (!ctx->Ublk) return set_err(ctx, RSVDT_ERR_OOM, "U allocation failed");
+    if (!cuda_ok(ctx, cudaMemcpyAsync(ctx->Ublk, ctx->blk, sizeof(z128) * n, cudaMemcpyDeviceToDevice, ctx->stream),
+                 "copy"))
+      return RSVDT_ERR_CUDA;
+    ctx->U_rows = rows;
+  } else {
+    if (!ctx->Ublk) return set_err(ctx, RSVDT_ERR_STATE, "U has not been stored (run the SVD before the adjoint first)");
+    dfree(ctx, ctx->Vblk);
+    ctx->Vblk = (z128 *)dalloc(ctx, sizeof(z128) * n);
+    if (!ctx->Vblk) return set_err(ctx, RSVDT_ERR_OOM, "V allocation failed");
+    RSVDT_TRY(svd_all(ctx, ctx->blk, rows, ctx->Nw_eff, ctx->K, ctx->Vblk, ctx->S));
+    // Inverse weights (SourceCode/SVDAllFreqs.c:63-64).
+    const int64_t C = ctx->Nw_eff * ctx->K;
+    if (ctx->W[RSVDT_W_Q_SQRT_INV].present) {
+      RSVDT_TRY(apply_weight(ctx, ctx->W[RSVDT_W_Q_SQRT_INV], ctx->Ublk, ctx->blk2, C));
+      if (!cuda_ok(ctx, cudaMemcpyAsync(ctx->Ublk, ctx->blk2, sizeof(z128) * ctx->U_rows * C,
+                                        cudaMemcpyDeviceToDevice, ctx->stream), "copy"))
+        return RSVDT_ERR_CUDA;
+    }
+    if (ctx->W[RSVDT_W_F_SQRT_INV].present) {
+      RSVDT_TRY(apply_weight(ctx, ctx->W[RSVDT_W_F_SQRT_INV], ctx->Vblk, ctx->blk2, C));
+      if (!cuda_ok(ctx, cudaMemcpyAsync(ctx->Vblk, ctx->blk2, sizeof(z128) * rows * C,
+                                        cudaMemcpyDeviceToDevice, ctx->stream), "copy"))
+        return RSVDT_ERR_CUDA;
+    }
+    ctx->have_results = true;
+  }
+  return cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
+}
+
+rsvdt_status rsvdt_power_iteration(rsvdt_ctx *ctx) {
+  RSVDT_TRY(require_ready(ctx, true));
+  for (int64_t iq = 0; iq < ctx->par.q; ++iq) {  // SourceCode/PowerIterationRK4.c:20-29
+    if (ctx->par.Display >= 1)
+      printf("\n******** Inside power iteration, %d/%d *******\n", (int)iq + 1, (int)ctx->par.q);
+    RSVDT_TRY(rsvdt_qr_all_freqs(ctx));
+    RSVDT_TRY(rsvdt_action(ctx, RSVDT_ADJOINT));
+    RSVDT_TRY(rsvdt_qr_all_freqs(ctx));
+    RSVDT_TRY(rsvdt_action(ctx, RSVDT_DIRECT));
+  }
+  return RSVDT_OK;
+}
+
+rsvdt_status rsvdt_run(rsvdt_ctx *ctx) {
+  RSVDT_TRY(require_ready(ctx, true));
+  RSVDT_TRY(rsvdt_action(ctx, RSVDT_DIRECT));      // SourceCode/main.c:134
+  RSVDT_TRY(rsvdt_power_iteration(ctx));           // :136
+  RSVDT_TRY(rsvdt_svd_all_freqs(ctx, 1));          // :138-140
+  RSVDT_TRY(rsvdt_action(ctx, RSVDT_ADJOINT));     // :142
+  RSVDT_TRY(rsvdt_svd_all_freqs(ctx, 0));          // :144
+  return RSVDT_OK;
+}
+
+rsvdt_status rsvdt_get_results(rsvdt_ctx *ctx, double *U, int64_t ldu, double *V, int64_t ldv, double *S) {
+  if (!ctx) return RSVDT_ERR_ARG;
+  if (!ctx->have_results) return set_err(ctx, RSVDT_ERR_STATE, "no results yet (call rsvdt_run)");
+  const int64_t C = ctx->Nw_eff * ctx->K;
+  auto fetch = [&](const z128 *src, int64_t rows, double *dst, int64_t ld) -> rsvdt_status {
+    if (!dst) return RSVDT_OK;
+    if (ld < rows) return set_err(ctx, RSVDT_ERR_ARG, "leading dimension too small");
+    z128 *stage = (z128 *)dalloc(ctx, sizeof(z128) * ld * C);
+    if (!stage) return set_err(ctx, RSVDT_ERR_OOM, "staging allocation failed");
+    rsvdt_status st = launch_blk_to_colmajor(ctx, src, rows, C, stage, ld);
+    if (!st && !cuda_ok(ctx, cudaMemcpyAsync(dst, stage, sizeof(z128) * ld * C, cudaMemcpyDeviceToHost, ctx->stream),
+                        "download"))
+      st = RSVDT_ERR_CUDA;
+    if (!st && !cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync")) st = RSVDT_ERR_CUDA;
+    dfree(ctx, stage);
+    return st;
+  };
+  RSVDT_TRY(fetch(ctx->Ublk, ctx->U_rows, U, ldu));
+  RSVDT_TRY(fetch(ctx->Vblk, ctx->Nb, V, ldv));
+  if (S && !cuda_ok(ctx, cudaMemcpy(S, ctx->S, sizeof(double) * C, cudaMemcpyDeviceToHost), "download"))
+    return RSVDT_ERR_CUDA;
+  return RSVDT_OK;
+}
+
+rsvdt_status rsvdt_rk4_reset(rsvdt_ctx *ctx, rsvdt_dir dir) {
+  RSVDT_TRY(require_ready(ctx, true));
+  if (ctx->blk_rows != ctx->N) return set_err(ctx, RSVDT_ERR_STATE, "working block must have N rows");
+  const int prec = ctx->par.precision;
+  ctx->Nstore = ctx->par.TransientRemoval ? ctx->Nw + 1 : ctx->Nw;
+  RSVDT_TRY(stage_forcing(ctx, prec));
+  RSVDT_TRY(launch_forcing_init(ctx, dir == RSVDT_DIRECT ? 1 : 0, prec));
+  return RSVDT_OK;
+}
+
+rsvdt_status rsvdt_rk4_advance(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps) {
+  RSVDT_TRY(require_ready(ctx, true));
+  if (i0 < 1 || nsteps < 0) return set_err(ctx, RSVDT_ERR_ARG, "invalid step range");
+  return run_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, ctx->par.precision, i0, nsteps, true);
+}
+
+rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps, double *y, double *F3) {
+  RSVDT_TRY(require_ready(ctx, true));
+  if (!y || !F3) return set_err(ctx, RSVDT_ERR_ARG, "null state");
+  if (ctx->blk_rows != ctx->N) return set_err(ctx, RSVDT_ERR_STATE, "working block must have N rows");
+  const int prec = ctx->par.precision;
+  const int64_t N = ctx->N, K = ctx->K;
+  ctx->Nstore = ctx->par.TransientRemoval ? ctx->Nw + 1 : ctx->Nw;
+  RSVDT_TRY(stage_forcing(ctx, prec));
+  z128 *stage = (z128 *)dalloc(ctx, sizeof(z128) * N * K * 2);
+  if (!stage) return set_err(ctx, RSVDT_ERR_OOM, "staging allocation failed");
+  rsvdt_status st = RSVDT_OK;
+  // Host (N x K column-major) -> device [n][k]; complex64 form rounds.
+  z128 *ytmp = stage + N * K;
+  auto to_dev = [&](const double *h, void *d) -> rsvdt_status {
+    if (!cuda_ok(ctx, cudaMemcpyAsync(stage, h, sizeof(z128) * N * K, cudaMemcpyHostToDevice, ctx->stream), "upload"))
+      return RSVDT_ERR_CUDA;
+    if (prec == RSVDT_PREC_C64) {
+      RSVDT_TRY(launch_colmajor_to_blk(ctx, stage, N, N, K, ytmp));
+      return launch_convert_to64(ctx, ytmp, (z64 *)d, N * K);
+    }
+    return launch_colmajor_to_blk(ctx, stage, N, N, K, (z128 *)d);
+  };
+  st = to_dev(y, ctx->y);
+  if (!st && !cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync")) st = RSVDT_ERR_CUDA;
+  if (!st) st = to_dev(F3, ctx->F3);
+  if (!st) st = run_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, prec, i0, nsteps, true);
+  auto to_host = [&](void *d, double *h) -> rsvdt_status {
+    const z128 *src = (const z128 *)d;
+    if (prec == RSVDT_PREC_C64) return set_err(ctx, RSVDT_ERR_ARG, "rsvdt_rk4_steps reads back complex128 state only");
+    RSVDT_TRY(launch_blk_to_colmajor(ctx, src, N, K, stage, N));
+    if (!cuda_ok(ctx, cudaMemcpyAsync(h, stage, sizeof(z128) * N * K, cudaMemcpyDeviceToHost, ctx->stream), "download"))
+      return RSVDT_ERR_CUDA;
+    return cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
+  };
+  if (!st) st = to_host(ctx->y, y);
+  if (!st) st = to_host(ctx->F3, F3);
+  dfree(ctx, stage);
+  return st;
+}
+
+rsvdt_status rsvdt_synchronize(rsvdt_ctx *ctx) {
+  if (!ctx) return RSVDT_ERR_ARG;
+  return cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
+}
+
+void *rsvdt_stream(rsvdt_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int64_t rsvdt_launch_count(const rsvdt_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,206 @@
+// Shared definitions of the GB300 RSVD-Delta-t library: complex arithmetic,
+// device buffers, the context, launch helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "rsvdt.h"
+
+namespace rsvdt {
+
+// ------------------------------------------------------------------ complex
+
+template <class R>
+struct cplx {
+  R re, im;
+};
+template <class R>
+struct alignas(2 * sizeof(R)) cplx_a {
+  R re, im;
+};
+using z128 = cplx_a<double>;  // 16-byte aligned complex128
+using z64 = cplx_a<float>;    // 8-byte aligned complex64
+
+template <class Z>
+struct real_of;
+template <>
+struct real_of<z128> {
+  using type = double;
+};
+template <>
+struct real_of<z64> {
+  using type = float;
+};
+
+template <class Z>
+__host__ __device__ __forceinline__ Z zmake(typename real_of<Z>::type r,
+                                            typename real_of<Z>::type i) {
+  Z z;
+  z.re = r;
+  z.im = i;
+  return z;
+}
+
+// acc += a * x (complex multiply-accumulate, 4 FMA).
+template <class Z>
+__device__ __forceinline__ void zmac(Z &acc, const Z a, const Z x) {
+  acc.re = fma(a.re, x.re, acc.re);
+  acc.re = fma(-a.im, x.im, acc.re);
+  acc.im = fma(a.re, x.im, acc.im);
+  acc.im = fma(a.im, x.re, acc.im);
+}
+// acc += conj(a) * x
+template <class Z>
+__device__ __forceinline__ void zmacc(Z &acc, const Z a, const Z x) {
+  acc.re = fma(a.re, x.re, acc.re);
+  acc.re = fma(a.im, x.im, acc.re);
+  acc.im = fma(a.re, x.im, acc.im);
+  acc.im = fma(-a.im, x.re, acc.im);
+}
+// s * x + y with real s (VecWAXPY / VecAXPY with a real coefficient).
+template <class Z>
+__device__ __forceinline__ Z zaxpy(typename real_of<Z>::type s, const Z x, const Z y) {
+  Z r;
+  r.re = fma(s, x.re, y.re);
+  r.im = fma(s, x.im, y.im);
+  return r;
+}
+template <class Z>
+__device__ __forceinline__ Z zmul(const Z a, const Z b) {
+  Z r;
+  r.re = a.re * b.re - a.im * b.im;
+  r.im = a.re * b.im + a.im * b.re;
+  return r;
+}
+
+// ---------------------------------------------------------------- buffers
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+// Device sparse matrix, CSR with int32 indices (rows, cols < 2^31).
+struct DevCSR {
+  bool present = false;
+  bool diag = false;  // nonzeros are exactly the diagonal
+  int64_t rows = 0, cols = 0, nnz = 0;
+  int32_t *rowptr = nullptr;
+  int32_t *col = nullptr;
+  z128 *val = nullptr;
+  z64 *val32 = nullptr;  // complex64 copy for the precision form
+};
+
+// Block-CSR operator with dense bs x bs blocks (row-major inside a block).
+struct DevBCSR {
+  bool present = false;
+  int32_t bs = 0;
+  int64_t nb = 0, nblocks = 0;
+  int32_t *browptr = nullptr;
+  int32_t *bcol = nullptr;
+  z128 *val = nullptr;
+  z64 *val32 = nullptr;
+};
+
+}  // namespace rsvdt
+
+struct rsvdt_ctx {
+  rsvdt_params par{};
+  // Derived grid (SourceCode/SetupTimeFreqGrid.c:16-21).
+  double w = 0, dt = 0;
+  int64_t Ns = 0, Nt = 0, R = 0, Nw = 0, Nw_eff = 0, K = 0;
+  int64_t N = 0, Nb = 0, Nc = 0;
+  bool real_op = false;
+  bool have_operator = false;
+  bool have_block = false;
+  bool have_results = false;
+
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+  std::string err;
+
+  // Operator and its conjugate transpose.
+  rsvdt::DevCSR A, AH;
+  rsvdt::DevBCSR BA, BAH;
+  rsvdt::DevCSR W[5], WH[5];
+
+  // Spectral blocks, layout [row][iw][k] (complex128).
+  int64_t blk_rows = 0;  // rows of the working block
+  rsvdt::z128 *blk = nullptr;
+  rsvdt::z128 *blk2 = nullptr;
+  rsvdt::z128 *Ublk = nullptr;
+  int64_t U_rows = 0;
+  rsvdt::z128 *Vblk = nullptr;
+  double *S = nullptr;  // [iw][k] gains
+  size_t blk_elems = 0; // capacity of blk/blk2 in complex values
+
+  // Forcing coefficients of the running action, [n][iw][k].
+  void *Fh = nullptr;
+  // RK4 state, each N*K interleaved [n][k].
+  void *y = nullptr, *zA = nullptr, *zB = nullptr, *acc = nullptr, *F2 = nullptr, *F3 = nullptr;
+  void *ring = nullptr;  // [Nstore][n][k]
+  int64_t Nstore = 0;
+  // Phasor tables: idft^T [2Ns][Nw_eff] (complex128 and complex64 copies),
+  // dft [Nw][Nw_eff].
+  rsvdt::z128 *tab = nullptr;
+  rsvdt::z64 *tab32 = nullptr;
+  rsvdt::z128 *dft = nullptr;
+  // Device step counters (see step.cu) and status flags.
+  int64_t *d_step = nullptr;
+  int32_t *d_flags = nullptr;
+  // Scratch for the dense stages.
+  void *scratch = nullptr;
+  size_t scratch_bytes = 0;
+
+  // Cached CUDA graphs of G RK4 steps per direction.
+  cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
+  int64_t step_graph_len = 0;
+
+  std::vector<void *> allocations;
+};
+
+namespace rsvdt {
+
+// Returns false and records the message when a CUDA call failed.
+bool cuda_ok(rsvdt_ctx *ctx, cudaError_t e, const char *what);
+rsvdt_status set_err(rsvdt_ctx *ctx, rsvdt_status s, const char *fmt, ...);
+// Allocates device memory tracked by the context (freed in rsvdt_destroy).
+void *dalloc(rsvdt_ctx *ctx, size_t bytes);
+void dfree(rsvdt_ctx *ctx, void *p);
+
+inline int grid_for(int64_t n, int threads) {
+  int64_t g = (n + threads - 1) / threads;
+  return (int)(g < 1 ? 1 : g);
+}
+
+// ------------------------------------------------- kernels (launchers)
+// step.cu
+rsvdt_status launch_forcing_init(rsvdt_ctx *ctx, int dir, int prec);
+rsvdt_status run_steps(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_t nsteps,
+                       bool sample);
+rsvdt_status launch_dft(rsvdt_ctx *ctx, int prec, z128 *out);
+rsvdt_status launch_unforced_steps(rsvdt_ctx *ctx, int dir, z128 *cols, int64_t ncols,
+                                   int64_t nsteps);
+// dense.cu
+rsvdt_status launch_colmajor_to_blk(rsvdt_ctx *ctx, const z128 *src, int64_t rows, int64_t ld,
+                                    int64_t C, z128 *dst);
+rsvdt_status launch_blk_to_colmajor(rsvdt_ctx *ctx, const z128 *src, int64_t rows, int64_t C,
+                                    z128 *dst, int64_t ld);
+rsvdt_status apply_weight(rsvdt_ctx *ctx, const DevCSR &M, const z128 *in, z128 *out,
+                          int64_t C);
+rsvdt_status cholqr2(rsvdt_ctx *ctx, z128 *blk, int64_t rows, int64_t nw, int64_t K,
+                     z128 *Rout);
+rsvdt_status svd_all(rsvdt_ctx *ctx, z128 *blk, int64_t rows, int64_t nw, int64_t K,
+                     z128 *Uout, double *S);
+rsvdt_status launch_random(rsvdt_ctx *ctx, z128 *dst, int64_t n, uint64_t seed);
+rsvdt_status launch_convert_to64(rsvdt_ctx *ctx, const z128 *src, z64 *dst, int64_t n);
+rsvdt_status check_finite(rsvdt_ctx *ctx, const z128 *p, int64_t n, bool *ok);
+rsvdt_status transient_removal(rsvdt_ctx *ctx, int dir, int prec, z128 *out);
+
+}  // namespace rsvdt

@@ -1,0 +1,286 @@
+"""Python binding of the GB300 RSVD-Delta-t C ABI (include/rsvdt.h).
+
+Mirrors the reference's hot-path interface (AliFarghadan/RSVD-Delta-t,
+SourceCode/main.c:134-144): a Context holds the operator, the weights and
+the working spectral block; `action`, `qr_all_freqs`, `svd_all_freqs`,
+`power_iteration` and `run` stand in for DirectActionRK4 /
+AdjointActionRK4, QRAllFreqs, SVDAllFreqs(BeforeAdjoint), PowerIterationRK4
+and the main sequence. Errors raise RsvdtError carrying the library's status
+code and message, as the reference's CHKERRQ/SETERRQ chain does.
+
+There is no CPU fallback: the shared library must have been built
+(`build.build_library`) and a CUDA device must be present.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB_PATH
+
+OK, ERR_ARG, ERR_IO, ERR_OOM, ERR_CUDA, ERR_NOT_SPD, ERR_DIVERGED, ERR_TIMEOUT, ERR_STATE = range(9)
+ADJOINT, DIRECT = 0, 1
+PREC_C128, PREC_C64 = 0, 1
+W_F_SQRT_INV, B, C_OUT, W_Q_SQRT, W_Q_SQRT_INV = range(5)
+
+STATUS_NAMES = {0: "OK", 1: "ARG", 2: "IO", 3: "OOM", 4: "CUDA", 5: "NOT_SPD", 6: "DIVERGED",
+                7: "TIMEOUT", 8: "STATE"}
+
+# Every symbol include/rsvdt.h declares.
+EXPORTED = [
+    "rsvdt_default_params", "rsvdt_create", "rsvdt_destroy", "rsvdt_last_error",
+    "rsvdt_set_operator", "rsvdt_set_operator_bcsr", "rsvdt_set_weight", "rsvdt_get_grid",
+    "rsvdt_set_sketch", "rsvdt_random_sketch", "rsvdt_get_block", "rsvdt_action",
+    "rsvdt_qr_all_freqs", "rsvdt_svd_all_freqs", "rsvdt_power_iteration", "rsvdt_run",
+    "rsvdt_get_results", "rsvdt_rk4_steps", "rsvdt_rk4_reset", "rsvdt_rk4_advance",
+    "rsvdt_synchronize", "rsvdt_stream", "rsvdt_launch_count",
+]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("k", C.c_int64), ("q", C.c_int64), ("Nw", C.c_int64), ("w", C.c_double),
+        ("TwoPI", C.c_int32), ("dt", C.c_double), ("TransientLength", C.c_double),
+        ("TransientRemoval", C.c_int32), ("DiscFlg", C.c_int32), ("beta", C.c_double),
+        ("precision", C.c_int32), ("Display", C.c_int32),
+    ]
+
+
+class Grid(C.Structure):
+    _fields_ = [
+        ("w", C.c_double), ("dt", C.c_double), ("Ns", C.c_int64), ("Nt", C.c_int64),
+        ("ResRatio", C.c_int64), ("Nw_eff", C.c_int64), ("N", C.c_int64), ("Nb", C.c_int64),
+        ("Nc", C.c_int64),
+    ]
+
+
+class RsvdtError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"rsvdt error {STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Loads lib/librsvdt.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"CUDA library {path} is missing: run build.build_library() first")
+    lib = C.CDLL(path)
+    P = C.POINTER
+    vp = C.c_void_p
+    d = P(C.c_double)
+    i64 = C.c_int64
+    sig = {
+        "rsvdt_default_params": (None, [P(Params)]),
+        "rsvdt_create": (C.c_int, [P(Params), P(vp)]),
+        "rsvdt_destroy": (None, [vp]),
+        "rsvdt_last_error": (C.c_char_p, [vp]),
+        "rsvdt_set_operator": (C.c_int, [vp, i64, P(i64), P(i64), d]),
+        "rsvdt_set_operator_bcsr": (C.c_int, [vp, i64, C.c_int32, P(i64), P(i64), d]),
+        "rsvdt_set_weight": (C.c_int, [vp, C.c_int, i64, i64, P(i64), P(i64), d]),
+        "rsvdt_get_grid": (C.c_int, [vp, P(Grid)]),
+        "rsvdt_set_sketch": (C.c_int, [vp, d, i64, i64]),
+        "rsvdt_random_sketch": (C.c_int, [vp, C.c_uint64]),
+        "rsvdt_get_block": (C.c_int, [vp, d, i64, P(i64)]),
+        "rsvdt_action": (C.c_int, [vp, C.c_int]),
+        "rsvdt_qr_all_freqs": (C.c_int, [vp]),
+        "rsvdt_svd_all_freqs": (C.c_int, [vp, C.c_int32]),
+        "rsvdt_power_iteration": (C.c_int, [vp]),
+        "rsvdt_run": (C.c_int, [vp]),
+        "rsvdt_get_results": (C.c_int, [vp, d, i64, d, i64, d]),
+        "rsvdt_rk4_steps": (C.c_int, [vp, C.c_int, i64, i64, d, d]),
+        "rsvdt_rk4_reset": (C.c_int, [vp, C.c_int]),
+        "rsvdt_rk4_advance": (C.c_int, [vp, C.c_int, i64, i64]),
+        "rsvdt_synchronize": (C.c_int, [vp]),
+        "rsvdt_stream": (vp, [vp]),
+        "rsvdt_launch_count": (i64, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def default_params(**kw) -> Params:
+    lib = load_library()
+    p = Params()
+    lib.rsvdt_default_params(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+def _csr_arrays(indptr, indices, data):
+    rp = np.ascontiguousarray(indptr, dtype=np.int64)
+    ci = np.ascontiguousarray(indices, dtype=np.int64)
+    va = np.ascontiguousarray(data, dtype=np.complex128)
+    return rp, ci, va
+
+
+class Context:
+    """One resolvent problem on the GPU (one CUDA stream, device-resident
+    operator, weights and spectral blocks)."""
+
+    def __init__(self, params: Params | None = None, **kw):
+        self._lib = load_library()
+        self._h = C.c_void_p()
+        p = params if params is not None else default_params(**kw)
+        self.params = p
+        st = self._lib.rsvdt_create(C.byref(p), C.byref(self._h))
+        if st != OK:
+            msg = self._lib.rsvdt_last_error(self._h).decode() if self._h else "create failed"
+            self.close()
+            raise RsvdtError(st, msg)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.rsvdt_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st: int):
+        if st != OK:
+            raise RsvdtError(st, self._lib.rsvdt_last_error(self._h).decode())
+
+    # -------------------------------------------------------- set-up
+    def set_operator(self, A) -> None:
+        """A: scipy.sparse matrix (converted to CSR) or (indptr, indices, data)."""
+        if hasattr(A, "tocsr"):
+            A = A.tocsr()
+            A.sort_indices()
+            n = A.shape[0]
+            rp, ci, va = _csr_arrays(A.indptr, A.indices, A.data)
+        else:
+            rp, ci, va = _csr_arrays(*A)
+            n = rp.size - 1
+        self._check(self._lib.rsvdt_set_operator(self._h, n, _iptr(rp), _iptr(ci), _dptr(va.view(np.float64))))
+
+    def set_operator_bcsr(self, browptr, bcol, blocks) -> None:
+        """blocks: (nblocks, bs, bs) complex array, row-major inside a block."""
+        rp = np.ascontiguousarray(browptr, dtype=np.int64)
+        bc = np.ascontiguousarray(bcol, dtype=np.int64)
+        bl = np.ascontiguousarray(blocks, dtype=np.complex128)
+        bs = bl.shape[1]
+        self._check(self._lib.rsvdt_set_operator_bcsr(self._h, rp.size - 1, bs, _iptr(rp), _iptr(bc),
+                                                      _dptr(bl.view(np.float64))))
+
+    def set_weight(self, which: int, M) -> None:
+        M = M.tocsr()
+        M.sort_indices()
+        rp, ci, va = _csr_arrays(M.indptr, M.indices, M.data)
+        self._check(self._lib.rsvdt_set_weight(self._h, which, M.shape[0], M.shape[1], _iptr(rp), _iptr(ci),
+                                               _dptr(va.view(np.float64))))
+
+    def grid(self) -> Grid:
+        g = Grid()
+        self._check(self._lib.rsvdt_get_grid(self._h, C.byref(g)))
+        return g
+
+    def set_sketch(self, F: np.ndarray) -> None:
+        """F: Nb x (k*Nw_eff) complex, frequency-major columns (iw*k + ik)."""
+        F = np.asfortranarray(F, dtype=np.complex128)
+        self._check(self._lib.rsvdt_set_sketch(self._h, F.ctypes.data_as(C.POINTER(C.c_double)), F.shape[0],
+                                               F.shape[1]))
+        self._k = F.shape[1] // self.grid().Nw_eff
+
+    def random_sketch(self, seed: int) -> None:
+        self._check(self._lib.rsvdt_random_sketch(self._h, seed))
+
+    # -------------------------------------------------------- algorithm
+    def action(self, direction: int) -> None:
+        self._check(self._lib.rsvdt_action(self._h, direction))
+
+    def qr_all_freqs(self) -> None:
+        self._check(self._lib.rsvdt_qr_all_freqs(self._h))
+
+    def svd_all_freqs(self, before_adjoint: bool) -> None:
+        self._check(self._lib.rsvdt_svd_all_freqs(self._h, 1 if before_adjoint else 0))
+
+    def power_iteration(self) -> None:
+        self._check(self._lib.rsvdt_power_iteration(self._h))
+
+    def run(self) -> None:
+        self._check(self._lib.rsvdt_run(self._h))
+
+    # -------------------------------------------------------- read back
+    def get_block(self) -> np.ndarray:
+        rows = C.c_int64()
+        self._check(self._lib.rsvdt_get_block(self._h, None, 1, C.byref(rows)))
+        g = self.grid()
+        k = self.k
+        out = np.zeros((rows.value, k * g.Nw_eff), dtype=np.complex128, order="F")
+        self._check(self._lib.rsvdt_get_block(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), rows.value,
+                                              C.byref(rows)))
+        return out
+
+    @property
+    def k(self) -> int:
+        return int(self._k) if hasattr(self, "_k") else int(self.params.k)
+
+    def get_results(self):
+        g = self.grid()
+        ncol = self.k * g.Nw_eff
+        U = np.zeros((g.Nc, ncol), dtype=np.complex128, order="F")
+        V = np.zeros((g.Nb, ncol), dtype=np.complex128, order="F")
+        S = np.zeros((self.k, g.Nw_eff), dtype=np.float64, order="F")
+        self._check(self._lib.rsvdt_get_results(self._h, U.ctypes.data_as(C.POINTER(C.c_double)), g.Nc,
+                                                V.ctypes.data_as(C.POINTER(C.c_double)), g.Nb,
+                                                S.ctypes.data_as(C.POINTER(C.c_double))))
+        return U, V, S
+
+    def rk4_steps(self, direction: int, i0: int, nsteps: int, y: np.ndarray, F3: np.ndarray):
+        """Advances the host state y, F3 (N x k complex, Fortran order) in place."""
+        y = np.asfortranarray(y, dtype=np.complex128)
+        F3 = np.asfortranarray(F3, dtype=np.complex128)
+        self._check(self._lib.rsvdt_rk4_steps(self._h, direction, i0, nsteps,
+                                              y.ctypes.data_as(C.POINTER(C.c_double)),
+                                              F3.ctypes.data_as(C.POINTER(C.c_double))))
+        return y, F3
+
+    def rk4_reset(self, direction: int) -> None:
+        self._check(self._lib.rsvdt_rk4_reset(self._h, direction))
+
+    def rk4_advance(self, direction: int, i0: int, nsteps: int) -> None:
+        self._check(self._lib.rsvdt_rk4_advance(self._h, direction, i0, nsteps))
+
+    def synchronize(self) -> None:
+        self._check(self._lib.rsvdt_synchronize(self._h))
+
+    def stream(self) -> int:
+        return int(self._lib.rsvdt_stream(self._h) or 0)
+
+    def launch_count(self) -> int:
+        return int(self._lib.rsvdt_launch_count(self._h))

@@ -1,0 +1,286 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle
+(the C restatement of the reference) on the same seeded inputs.
+
+Tolerances (floating point, complex128 plain form): the spec bar is a
+relative gain error <= 1e-9 and subspace angles <= 1e-7 rad against the
+reference's own run; against the restatement, which performs the same
+operations in the same order up to FMA contraction and summation order, the
+tests demand more where the mathematics allows it (see each test).
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import oracle
+from rsvdt import synth
+
+pytestmark = pytest.mark.gpu
+
+GAIN_TOL = 1e-9
+ANGLE_TOL = 1e-7
+
+
+def small_gl(N=64, w=0.1, Nw=16, dt_in=0.15, TL_periods=1.0):
+    """Stable 64-node Ginzburg-Landau operator (mu0 = 0.2: max Re(lambda) =
+    -0.108, |lambda| <= 12.3, RK4-stable at dt = 0.145)."""
+    A = synth.gl_operator(N, mu0=0.2)
+    T = 2 * np.pi / w
+    return A, dict(w=w, Nw=Nw, dt=dt_in, TransientLength=TL_periods * T)
+
+
+def make_ctx(A, cfg, k, q=0, tr=False, prec=0, bcsr=None):
+    import rsvdt
+    p = rsvdt.default_params(k=k, q=q, Nw=cfg["Nw"], w=cfg["w"], dt=cfg["dt"],
+                             TransientLength=cfg["TransientLength"], TransientRemoval=int(tr),
+                             precision=prec, Display=0)
+    ctx = rsvdt.Context(p)
+    if bcsr is not None:
+        ctx.set_operator_bcsr(*bcsr)
+    else:
+        ctx.set_operator(A)
+    return ctx
+
+
+def make_oracle(A, cfg, tr=False):
+    return oracle.Oracle(A, cfg["Nw"], cfg["w"], cfg["dt"], cfg["TransientLength"], transient_removal=tr)
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def angles(U, Uref, k, nw, jmax):
+    """Angle between u and u_ref (unit vectors after the best unit-modulus
+    phase) per (frequency, mode j < jmax); columns iw*k + j. Computed from
+    the chord 2 sin(theta/2) = |u - e^{i phi} u_ref|, which stays accurate
+    below 1e-8 where arccos|<u, u_ref>| does not."""
+    out = np.zeros((jmax, nw))
+    for iw in range(nw):
+        for j in range(jmax):
+            u = U[:, iw * k + j] / np.linalg.norm(U[:, iw * k + j])
+            v = Uref[:, iw * k + j] / np.linalg.norm(Uref[:, iw * k + j])
+            c = np.vdot(v, u)
+            ph = c / abs(c) if abs(c) > 0 else 1.0
+            out[j, iw] = 2 * np.arcsin(min(1.0, np.linalg.norm(u - ph * v) / 2))
+    return out
+
+
+def test_grid_matches_oracle(built_lib):
+    A, cfg = small_gl()
+    ctx = make_ctx(A, cfg, k=2)
+    g = ctx.grid()
+    dt, Ns, Nt, R = oracle.setup_grid(cfg["w"], cfg["Nw"], cfg["dt"], cfg["TransientLength"])
+    assert (g.Ns, g.Nt, g.ResRatio) == (Ns, Nt, R)
+    assert g.dt == dt
+    ctx.close()
+
+
+@pytest.mark.parametrize("direction", [1, 0])
+def test_rk4_steps_match_oracle(built_lib, direction):
+    """A window of forced RK4 steps (SourceCode/TSRK4.c) from a random
+    state, past the period wrap of the forcing index."""
+    A, cfg = small_gl()
+    k = 3
+    ctx = make_ctx(A, cfg, k=k)
+    g = ctx.grid()
+    N, nwe = A.shape[0], g.Nw_eff
+    F = synth.complex_normal(N, k * nwe, 5)
+    y0 = synth.complex_normal(N, k, 6)
+    F30 = synth.complex_normal(N, k, 7)
+    ctx.set_sketch(F)
+    i0 = 2 * g.Ns - 7  # crosses jt = 2Ns -> 0
+    y, F3 = ctx.rk4_steps(direction, i0, 20, y0.copy(), F30.copy())
+    orc = make_oracle(A, cfg)
+    for ik in range(k):
+        Fk = F[:, [iw * k + ik for iw in range(nwe)]]
+        yo, F3o = orc.rk4_steps(direction, Fk, i0, 20, y0[:, ik], F30[:, ik])
+        assert rel(y[:, ik], yo) < 1e-13
+        assert rel(F3[:, ik], F3o) < 1e-13
+    ctx.close()
+
+
+@pytest.mark.parametrize("direction,tr", [(1, False), (0, False), (1, True), (0, True)])
+def test_action_matches_oracle(built_lib, direction, tr):
+    """One resolvent action (TSActionRK4 + DFT or transient removal)."""
+    A, cfg = small_gl()
+    k = 3
+    ctx = make_ctx(A, cfg, k=k, tr=tr)
+    g = ctx.grid()
+    F = synth.complex_normal(A.shape[0], k * g.Nw_eff, 21)
+    ctx.set_sketch(F)
+    ctx.action(direction)
+    Y = ctx.get_block()
+    Yo = make_oracle(A, cfg, tr=tr).ts_action(direction, F)
+    # Per frequency block relative error.
+    for iw in range(g.Nw_eff):
+        blk = slice(iw * k, (iw + 1) * k)
+        assert rel(Y[:, blk], Yo[:, blk]) < (1e-11 if not tr else 1e-9), iw
+    ctx.close()
+
+
+def test_qr_and_svd_match_oracle(built_lib):
+    A, cfg = small_gl()
+    k = 4
+    ctx = make_ctx(A, cfg, k=k)
+    g = ctx.grid()
+    Y = synth.complex_normal(A.shape[0], k * g.Nw_eff, 3)
+    # Make some blocks ill-conditioned (kappa ~ 1e4).
+    Y[:, 0] *= 1e-4
+    ctx.set_sketch(Y)
+    ctx.qr_all_freqs()
+    Q = ctx.get_block()
+    Qo = oracle.qr_all_freqs(Y, k)
+    assert rel(Q, Qo) < 1e-11
+    for iw in range(g.Nw_eff):
+        b = Q[:, iw * k:(iw + 1) * k]
+        assert np.abs(b.conj().T @ b - np.eye(k)).max() < 1e-13
+    # SVD before the adjoint: the block becomes the left singular vectors.
+    ctx.set_sketch(Y)
+    ctx.svd_all_freqs(True)
+    U = ctx.get_block()
+    Uo, So = oracle.svd_all_freqs(Y, k)
+    ang = angles(U, Uo, k, g.Nw_eff, k)
+    assert ang.max() < 1e-9
+    ctx.close()
+
+
+@pytest.mark.parametrize("q,tr", [(0, False), (1, True)])
+def test_run_matches_oracle(built_lib, q, tr):
+    """The whole main.c sequence (SourceCode/main.c:134-144)."""
+    A, cfg = small_gl()
+    k = 3
+    ctx = make_ctx(A, cfg, k=k, q=q, tr=tr)
+    g = ctx.grid()
+    F = synth.complex_normal(A.shape[0], k * g.Nw_eff, 14)
+    ctx.set_sketch(F)
+    ctx.run()
+    U, V, S = ctx.get_results()
+    Uo, Vo, So = make_oracle(A, cfg, tr=tr).run(F, q)
+    assert np.abs(S - So).max() / So.max() < GAIN_TOL
+    assert (np.abs(S - So) / So).max() < 1e-7
+    assert angles(U, Uo, k, g.Nw_eff, 1).max() < ANGLE_TOL
+    assert angles(V, Vo, k, g.Nw_eff, 1).max() < ANGLE_TOL
+    ctx.close()
+
+
+def test_weights_match_oracle(built_lib):
+    """Diagonal W_q^{1/2}, W_f^{-1/2}, W_q^{-1/2} and rectangular B, C
+    (SourceCode/ApplyWeightMats.c, SourceCode/SVDAllFreqs.c:63-64)."""
+    import rsvdt
+    A, cfg = small_gl()
+    N = A.shape[0]
+    k = 2
+    rng = np.random.default_rng(3)
+    Nb, Nc = 40, 30
+    Bm = sp.random(N, Nb, density=0.1, random_state=1, dtype=np.float64).astype(np.complex128) + \
+        sp.eye(N, Nb, dtype=np.complex128)
+    Cm = sp.random(Nc, N, density=0.1, random_state=2, dtype=np.float64).astype(np.complex128) + \
+        sp.eye(Nc, N, dtype=np.complex128)
+    wf = rng.uniform(0.5, 1.5, Nb)
+    wq = rng.uniform(0.5, 1.5, Nc)
+    Wf_inv = sp.diags(1 / np.sqrt(wf) + 0j, format="csr")
+    Wq = sp.diags(np.sqrt(wq) + 0j, format="csr")
+    Wq_inv = sp.diags(1 / np.sqrt(wq) + 0j, format="csr")
+    ctx = make_ctx(A, cfg, k=k, q=1)
+    orc = make_oracle(A, cfg)
+    for which, M in [(rsvdt.W_F_SQRT_INV, Wf_inv), (rsvdt.B, Bm), (rsvdt.C_OUT, Cm), (rsvdt.W_Q_SQRT, Wq),
+                     (rsvdt.W_Q_SQRT_INV, Wq_inv)]:
+        ctx.set_weight(which, M)
+        orc.set_weight(which, M)
+    g = ctx.grid()
+    assert (g.Nb, g.Nc) == (Nb, Nc)
+    F = synth.complex_normal(Nb, k * g.Nw_eff, 8)
+    ctx.set_sketch(F)
+    ctx.run()
+    U, V, S = ctx.get_results()
+    Uo, Vo, So = orc.run(F, 1)
+    assert U.shape == (Nc, k * g.Nw_eff) and V.shape == (Nb, k * g.Nw_eff)
+    assert (np.abs(S - So) / So).max() < 1e-8
+    assert angles(U, Uo, k, g.Nw_eff, 1).max() < ANGLE_TOL
+    assert angles(V, Vo, k, g.Nw_eff, 1).max() < ANGLE_TOL
+    ctx.close()
+
+
+def test_bcsr_matches_csr_and_oracle(built_lib):
+    """Block-CSR operator (3D five-field shape, 4^3 grid) against the same
+    operator as CSR on the GPU and in the oracle."""
+    br, bc, bl = synth.op3d_blocks(n=4, shift=0.5, seed=3)
+    Acsr = synth.bcsr_to_csr(br, bc, bl)
+    cfg = dict(w=0.5, Nw=8, dt=0.05, TransientLength=2 * np.pi / 0.5)
+    k = 2
+    ctx_b = make_ctx(None, cfg, k=k, bcsr=(br, bc, bl))
+    ctx_c = make_ctx(Acsr, cfg, k=k)
+    g = ctx_b.grid()
+    F = synth.complex_normal(Acsr.shape[0], k * g.Nw_eff, 9)
+    for d in (1, 0):
+        ctx_b.set_sketch(F)
+        ctx_c.set_sketch(F)
+        ctx_b.action(d)
+        ctx_c.action(d)
+        Yb, Yc = ctx_b.get_block(), ctx_c.get_block()
+        Yo = make_oracle(Acsr, cfg).ts_action(d, F)
+        assert rel(Yb, Yc) < 1e-12
+        assert rel(Yb, Yo) < 1e-11
+    ctx_b.close()
+    ctx_c.close()
+
+
+def test_c64_form_close_to_c128(built_lib):
+    """Precision form: complex64 operator/state/stages with FP32 accumulation,
+    FP64 DFT/QR/SVD. Gains within 1e-3 of the complex128 plain form."""
+    A, cfg = small_gl()
+    k = 3
+    g128 = make_ctx(A, cfg, k=k, q=1, tr=True)
+    g64 = make_ctx(A, cfg, k=k, q=1, tr=True, prec=1)
+    F = synth.complex_normal(A.shape[0], k * g128.grid().Nw_eff, 14)
+    for c in (g128, g64):
+        c.set_sketch(F)
+        c.run()
+    _, _, S128 = g128.get_results()
+    _, _, S64 = g64.get_results()
+    assert (np.abs(S64 - S128) / S128)[0].max() < 1e-3
+    g128.close()
+    g64.close()
+
+
+def test_diverged_and_state_errors(built_lib):
+    import rsvdt
+    A, cfg = small_gl()
+    # Strongly unstable operator: the response overflows to Inf/NaN.
+    Abad = A + sp.eye(A.shape[0]) * 40.0
+    ctx = make_ctx(Abad, cfg, k=1)
+    with pytest.raises(rsvdt.RsvdtError) as e:
+        ctx.action(1)  # no sketch yet
+    assert e.value.status == rsvdt.ERR_STATE
+    F = synth.complex_normal(A.shape[0], ctx.grid().Nw_eff, 1)
+    with pytest.raises(rsvdt.RsvdtError) as e:
+        ctx.set_sketch(F[:, :-1])
+    assert e.value.status == rsvdt.ERR_ARG
+    ctx.set_sketch(F)
+    with pytest.raises(rsvdt.RsvdtError) as e:
+        ctx.action(1)
+    assert e.value.status == rsvdt.ERR_DIVERGED
+    ctx.close()
+
+
+@pytest.mark.parametrize("q,tr", [(0, False), (1, True)])
+def test_gl1_config_matches_oracle(built_lib, q, tr):
+    """The Ginzburg-Landau benchmark configuration at full size: N=500,
+    k=10, 64 frequencies j*0.1 (j=-32..31), dt=T/4096, one transient
+    period, q in {0, 1}."""
+    A = synth.gl_operator(500)
+    dt, T = synth.gl_time_grid(0.1, 4096)
+    cfg = dict(w=0.1, Nw=64, dt=dt, TransientLength=T)
+    k = 10
+    ctx = make_ctx(A, cfg, k=k, q=q, tr=tr)
+    g = ctx.grid()
+    assert (g.Ns, g.Nt, g.ResRatio) == (4096, 4096, 64)
+    F = synth.gl_sketch(500, k, 64, seed=14)
+    ctx.set_sketch(F)
+    ctx.run()
+    U, V, S = ctx.get_results()
+    Uo, Vo, So = make_oracle(A, cfg, tr=tr).run(F, q)
+    assert (np.abs(S - So) / So)[:3].max() < GAIN_TOL
+    assert angles(U, Uo, k, 64, 1).max() < ANGLE_TOL
+    assert angles(V, Vo, k, 64, 1).max() < ANGLE_TOL
+    ctx.close()
