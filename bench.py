@@ -1,0 +1,328 @@
+"""Benchmark of the RSVD-Delta-t RK4 hot path on one GB300.
+
+A "step" is one forced RK4 step (SourceCode/TSRK4.c: four sparse products
+with the forcing synthesis, stage updates and sampling fused into four
+kernels) over all k = 10 test vectors of the 3D64 five-field operator
+(N = 1,310,720, 45.26M complex128 nonzeros in 5x5 blocks, 32 frequencies),
+the plain complex128 form. The metric is the step's algorithmic HBM
+traffic over its device time:
+    B_step = 4 S_A + S_F + 19 S_v + S_v / R
+(S_A operator bytes, S_F = N Nw k 16 forcing coefficients, S_v = N k 16).
+Inputs (14 GB working set) are far larger than L2, so no flush is needed.
+
+Extra keys: roofline of the dominant kernel (stage 1, timed live with CUDA
+events on the library's stream), the FP64 rate it achieves against a
+measured FP64 peak (the plain form is FP64-bound on this part), the
+complex64 precision form's step, e2e through the C ABI with host buffers,
+and the CPU baseline (the C restatement timed on the host cores).
+
+--impl reference times the reference's CPU algorithm (the C restatement
+in oracle/, since the reference itself needs PETSc/SLEPc/MPI) on all host
+threads for the same step and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "rsvd-delta-t_gb300", "python")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "time-to-gains at ≤1e-3 rel err: chosen vs plain GPU; RK4 SpMM HBM GB/s vs peak"
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_peak_tflops(torch):
+    """FP64 peak of this GPU, measured: best of 5 cuBLAS DGEMMs 4096^3."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e))
+    del a, b
+    return 2 * 4096**3 / (best * 1e-3) / 1e12
+
+
+def cpu_baseline(wl, g, Fk, steps: int, threads: int):
+    """C restatement (oracle/) timing one step of all k test vectors, one
+    thread per test vector (ctypes releases the GIL)."""
+    import oracle
+    from rsvdt import synth
+
+    A = synth.bcsr_to_csr(*wl.bcsr) if wl.bcsr is not None else wl.csr
+    orc = oracle.Oracle(A, wl.Nw, wl.w, wl.dt_in, wl.transient_length)
+    N = wl.N
+    y = [np.zeros(N, complex) for _ in range(wl.k)]
+    F3 = [np.zeros(N, complex) for _ in range(wl.k)]
+    times = []
+    for s in range(steps):
+        t0 = time.perf_counter()
+        ths = []
+        for ik in range(wl.k):
+            def run(ik=ik):
+                y[ik], F3[ik] = orc.rk4_steps(1, Fk, 1 + s, 1, y[ik], F3[ik])
+            ths.append(threading.Thread(target=run))
+        # At most `threads` at a time.
+        for i in range(0, len(ths), threads):
+            for t in ths[i:i + threads]:
+                t.start()
+            for t in ths[i:i + threads]:
+                t.join()
+        times.append(time.perf_counter() - t0)
+    orc.close()
+    return float(np.mean(times))
+
+
+def run_reference(args):
+    """CPU arm: the reference algorithm on the host cores (oracle port)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from rsvdt import workloads
+    wl = workloads.make_3d(n=args.n)
+    import oracle
+    dt, Ns, Nt, R = oracle.setup_grid(wl.w, wl.Nw, wl.dt_in, wl.transient_length)
+    Fk = np.asfortranarray(np.random.default_rng(1).standard_normal((wl.N, wl.Nw)) + 0j)
+    threads = min(os.cpu_count() or 1, wl.k)
+    for _ in range(args.warmup if args.warmup <= 1 else 1):
+        cpu_baseline(wl, None, Fk, 1, threads)
+    t = cpu_baseline(wl, None, Fk, max(1, min(args.steps, 3)), threads)
+    b = wl.step_bytes(R)
+    val = b["step"] / t / 1e9
+    out = {"impl": "reference", "metric": METRIC, "value": round(val, 3), "unit": "GB/s", "n_gpus": args.gpus,
+           "steps": max(1, min(args.steps, 3)), "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+           "config": {"workload": f"{wl.name} five-field block operator, k={wl.k}, Nw={wl.Nw}, one forced RK4 step",
+                      "N": wl.N, "nnz": wl.meta["nnz"], "k": wl.k, "Nw": wl.Nw},
+           "cpu_baseline": {"value": round(val, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+                            "sample": f"{max(1, min(args.steps, 3))} steps x {wl.k} test vectors, one thread each; "
+                                      "C restatement of SourceCode/TSRK4.c (PETSc/SLEPc/MPI absent)"},
+           "e2e": {"value": round(val, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=64, help="3D grid size (64 for the benchmark)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    import rsvdt
+    from rsvdt import workloads
+
+    wl = workloads.make_3d(n=args.n)
+    ctx = rsvdt.Context(wl.params(precision=rsvdt.PREC_C128))
+    ctx.set_operator_bcsr(*wl.bcsr)
+    g = ctx.grid()
+    ctx.random_sketch(1234 + rank)
+    b = wl.step_bytes(g.ResRatio)
+    fl = wl.step_flops()
+    def timed(c, i0, n):
+        """CUDA events on the context's own stream around n device steps."""
+        stream = torch.cuda.ExternalStream(c.stream())
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        c.rk4_advance(rsvdt.DIRECT, i0, n)
+        e.record(stream)
+        e.synchronize()
+        return s.elapsed_time(e)
+
+    ctx.rk4_reset(rsvdt.DIRECT)
+    ctx.rk4_advance(rsvdt.DIRECT, 1, args.warmup)
+    ctx.synchronize()
+    launches0 = ctx.launch_count()
+    clocks = ClockSampler()
+    clocks.start()
+    time.sleep(1.5)  # let nvidia-smi start sampling before the timed region
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ms = timed(ctx, 1 + args.warmup, args.steps)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = ctx.launch_count() - launches0
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * b["step"] / (ms_step * 1e-3) / 1e9
+
+    # Dominant kernel: stage 1 timed launch by launch.
+    nprof = 5
+    st_ms = ctx.rk4_profile(rsvdt.DIRECT, 1 + args.warmup + args.steps, nprof)
+    st_ms = [x / nprof for x in st_ms]
+    hbm, peak_kind = peaks()
+    ach = b["stage1"] / (st_ms[0] * 1e-3) / 1e9
+    fp64_peak = fp64_peak_tflops(torch)
+    ach_fp64 = fl["stage1"] / (st_ms[0] * 1e-3) / 1e12
+    step_fp64 = fl["step"] / (ms_step * 1e-3) / 1e12
+
+    # e2e through the C ABI with host (pinned) state buffers: every call
+    # copies y and F3 in and out and restages the forcing block.
+    e2e_steps = 3
+    yh = torch.zeros((wl.k, wl.N), dtype=torch.complex128, pin_memory=True)
+    fh = torch.zeros((wl.k, wl.N), dtype=torch.complex128, pin_memory=True)
+    ynp, fnp = yh.numpy().T, fh.numpy().T  # N x k, Fortran order views
+    ctx.rk4_steps(rsvdt.DIRECT, 1, 1, ynp, fnp)
+    t0 = time.perf_counter()
+    for s in range(e2e_steps):
+        ctx.rk4_steps(rsvdt.DIRECT, 2 + s, 1, ynp, fnp)
+    e2e_t = (time.perf_counter() - t0) / e2e_steps
+    io_bytes = 2 * wl.N * wl.k * 16
+
+    # Precision form (complex64 stages, FP32 accumulation) on the same shape.
+    ctx64 = rsvdt.Context(wl.params(precision=rsvdt.PREC_C64))
+    ctx64.set_operator_bcsr(*wl.bcsr)
+    ctx64.random_sketch(1234 + rank)
+    ctx64.rk4_reset(rsvdt.DIRECT)
+    ctx64.rk4_advance(rsvdt.DIRECT, 1, 3)
+    ms64 = timed(ctx64, 4, args.steps) / args.steps
+    b64 = wl.step_bytes(g.ResRatio, s_c=8)
+    st64 = [x / nprof for x in ctx64.rk4_profile(rsvdt.DIRECT, 4 + args.steps, nprof)]
+    ctx64.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        Fk = np.asfortranarray(np.random.default_rng(1).standard_normal((wl.N, wl.Nw)) + 0j)
+        threads = min(os.cpu_count() or 1, wl.k)
+        t_cpu = cpu_baseline(wl, g, Fk, 2, threads)
+        cpu = {"value": round(b["step"] / t_cpu / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+               "sample": f"2 steps x {wl.k} test vectors of the same 3D64 step, one thread per test vector "
+                         f"({t_cpu:.2f} s/step); C restatement of SourceCode/TSRK4.c"}
+    ctx.close()
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded operator and sketch)",
+            "config": {"workload": f"{wl.name}: one forced RK4 step over k={wl.k} test vectors of the five-field "
+                                   f"64^3 block operator (5x5 blocks), Nw={wl.Nw}, complex128",
+                       "N": wl.N, "nnz": wl.meta["nnz"], "k": wl.k, "Nw": wl.Nw, "dt": g.dt, "Ns": g.Ns,
+                       "ResRatio": g.ResRatio, "step_bytes": b["step"], "l2": "working set 14 GB >> L2, no flush",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "kernel": "k_stage<z128,1> (SpMM + forcing synthesis)",
+                         "achieved": round(ach, 2), "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4),
+                         "peak_kind": peak_kind, "traffic": None,
+                         "bytes_per_launch": b["stage1"], "ms_per_launch": round(st_ms[0], 4),
+                         "fp64": {"achieved_tflops": round(ach_fp64, 4), "peak_tflops": round(fp64_peak, 4),
+                                  "frac": round(ach_fp64 / fp64_peak, 4),
+                                  "note": "plain complex128 form is FP64-bound on GB300; peak = cuBLAS DGEMM"}},
+            "stage_ms": [round(x, 4) for x in st_ms],
+            "step_fp64_tflops": round(step_fp64, 4),
+            "precision_form_c64": {"ms_per_step": round(ms64, 4),
+                                   "value": round(b64["step"] / (ms64 * 1e-3) / 1e9, 3), "unit": "GB/s",
+                                   "frac": round(b64["step"] / (ms64 * 1e-3) / 1e9 / hbm, 4),
+                                   "stage_ms": [round(x, 4) for x in st64],
+                                   "speedup_vs_c128": round(ms_step / ms64, 3)},
+            "clocks": clk,
+            "gpu_launches": int(launches),
+            "e2e": {"value": round(b["step"] / e2e_t / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": io_bytes,
+                    "d2h_bytes_per_step": io_bytes, "ms_per_step": round(e2e_t * 1e3, 3),
+                    "api": "rsvdt_rk4_steps (host y, F3 in pinned memory)"},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

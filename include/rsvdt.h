@@ -186,6 +186,13 @@ rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t 
 rsvdt_status rsvdt_rk4_reset(rsvdt_ctx *ctx, rsvdt_dir dir);
 rsvdt_status rsvdt_rk4_advance(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps);
 
+/* Runs nsteps device-resident steps (as rsvdt_rk4_advance) launching the
+ * four RK4 stage kernels one by one with CUDA events between them on the
+ * context's stream; stage_ms[0..3] receive each stage's total time in
+ * milliseconds. For benchmarks and roofline measurements. */
+rsvdt_status rsvdt_rk4_profile(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps,
+                               double *stage_ms);
+
 /* Waits for the context's stream. */
 rsvdt_status rsvdt_synchronize(rsvdt_ctx *ctx);
 

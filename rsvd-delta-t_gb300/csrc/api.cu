@@ -806,6 +806,12 @@ rsvdt_status rsvdt_rk4_advance(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_
   return run_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, ctx->par.precision, i0, nsteps, true);
 }
 
+rsvdt_status rsvdt_rk4_profile(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps, double *stage_ms) {
+  RSVDT_TRY(require_ready(ctx, true));
+  if (i0 < 1 || nsteps < 1 || !stage_ms) return set_err(ctx, RSVDT_ERR_ARG, "invalid profile arguments");
+  return profile_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, ctx->par.precision, i0, nsteps, stage_ms);
+}
+
 rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps, double *y, double *F3) {
   RSVDT_TRY(require_ready(ctx, true));
   if (!y || !F3) return set_err(ctx, RSVDT_ERR_ARG, "null state");

@@ -184,6 +184,8 @@ inline int grid_for(int64_t n, int threads) {
 rsvdt_status launch_forcing_init(rsvdt_ctx *ctx, int dir, int prec);
 rsvdt_status run_steps(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_t nsteps,
                        bool sample);
+rsvdt_status profile_steps(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_t nsteps,
+                           double *stage_ms);
 rsvdt_status launch_dft(rsvdt_ctx *ctx, int prec, z128 *out);
 rsvdt_status launch_unforced_steps(rsvdt_ctx *ctx, int dir, z128 *cols, int64_t ncols,
                                    int64_t nsteps);

@@ -14,7 +14,9 @@
 //  - SVDAllFreqs (SourceCode/SVDAllFreqs.c:34-56) becomes CholQR2 (Y = QR)
 //    followed by a one-sided Jacobi SVD of each k x k R (R = U_R S W^H) and
 //    U = Q U_R.
+#include <algorithm>
 #include <cmath>
+#include <cstdarg>
 
 #include "common.cuh"
 
@@ -747,3 +749,4 @@ rsvdt_status transient_removal(rsvdt_ctx *ctx, int dir, int prec, z128 *out) {
 }
 
 }  // namespace rsvdt
+

@@ -267,6 +267,54 @@ rsvdt_status run_steps(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_t ns
   return run_steps_t<z128>(ctx, dir, i0, nsteps);
 }
 
+// Steps launched one stage at a time with CUDA events between the stage
+// launches on the context's stream; stage_ms[s] accumulates the duration
+// of stage s+1 over the steps.
+template <class Z>
+static rsvdt_status profile_steps_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t nsteps,
+                                    double *stage_ms) {
+  auto P = make_args<Z>(ctx, dir, true);
+  const int th = 256;
+  const int g = grid_for(P.N * P.K, th);
+  cudaEvent_t ev[5];
+  for (auto &e : ev)
+    if (!cuda_ok(ctx, cudaEventCreate(&e), "event create")) return RSVDT_ERR_CUDA;
+  k_set_step<<<1, 1, 0, ctx->stream>>>(ctx->d_step, i0);
+  ctx->launches += 1;
+  for (int s = 0; s < 4; ++s) stage_ms[s] = 0;
+  rsvdt_status st = RSVDT_OK;
+  for (int64_t n = 0; n < nsteps && st == RSVDT_OK; ++n) {
+    cudaEventRecord(ev[0], ctx->stream);
+    k_stage<Z, 1><<<g, th, 0, ctx->stream>>>(P);
+    cudaEventRecord(ev[1], ctx->stream);
+    k_stage<Z, 2><<<g, th, 0, ctx->stream>>>(P);
+    cudaEventRecord(ev[2], ctx->stream);
+    k_stage<Z, 3><<<g, th, 0, ctx->stream>>>(P);
+    cudaEventRecord(ev[3], ctx->stream);
+    k_stage<Z, 4><<<g, th, 0, ctx->stream>>>(P);
+    cudaEventRecord(ev[4], ctx->stream);
+    ctx->launches += 4;
+    if (!cuda_ok(ctx, cudaEventSynchronize(ev[4]), "event sync")) {
+      st = RSVDT_ERR_CUDA;
+      break;
+    }
+    for (int s = 0; s < 4; ++s) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev[s], ev[s + 1]);
+      stage_ms[s] += ms;
+    }
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (st == RSVDT_OK && !cuda_ok(ctx, cudaGetLastError(), "profile steps")) st = RSVDT_ERR_CUDA;
+  return st;
+}
+
+rsvdt_status profile_steps(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_t nsteps,
+                           double *stage_ms) {
+  if (prec == RSVDT_PREC_C64) return profile_steps_t<z64>(ctx, dir, i0, nsteps, stage_ms);
+  return profile_steps_t<z128>(ctx, dir, i0, nsteps, stage_ms);
+}
+
 // DFT of the sampled period (SourceCode/DFT.c:26-38), FP64 sums:
 // out[n][iw][k] = ResRatio * sum_p ring[p][n][k] * dft[p][iw].
 template <class Z>

@@ -37,7 +37,7 @@ EXPORTED = [
     "rsvdt_set_sketch", "rsvdt_random_sketch", "rsvdt_get_block", "rsvdt_action",
     "rsvdt_qr_all_freqs", "rsvdt_svd_all_freqs", "rsvdt_power_iteration", "rsvdt_run",
     "rsvdt_get_results", "rsvdt_rk4_steps", "rsvdt_rk4_reset", "rsvdt_rk4_advance",
-    "rsvdt_synchronize", "rsvdt_stream", "rsvdt_launch_count",
+    "rsvdt_rk4_profile", "rsvdt_synchronize", "rsvdt_stream", "rsvdt_launch_count",
 ]
 
 
@@ -101,6 +101,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "rsvdt_rk4_steps": (C.c_int, [vp, C.c_int, i64, i64, d, d]),
         "rsvdt_rk4_reset": (C.c_int, [vp, C.c_int]),
         "rsvdt_rk4_advance": (C.c_int, [vp, C.c_int, i64, i64]),
+        "rsvdt_rk4_profile": (C.c_int, [vp, C.c_int, i64, i64, d]),
         "rsvdt_synchronize": (C.c_int, [vp]),
         "rsvdt_stream": (vp, [vp]),
         "rsvdt_launch_count": (i64, [vp]),
@@ -275,6 +276,13 @@ class Context:
 
     def rk4_advance(self, direction: int, i0: int, nsteps: int) -> None:
         self._check(self._lib.rsvdt_rk4_advance(self._h, direction, i0, nsteps))
+
+    def rk4_profile(self, direction: int, i0: int, nsteps: int) -> list:
+        """Per-stage device time (ms, summed over nsteps) from CUDA events."""
+        out = np.zeros(4)
+        self._check(self._lib.rsvdt_rk4_profile(self._h, direction, i0, nsteps,
+                                                out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out.tolist()
 
     def synchronize(self) -> None:
         self._check(self._lib.rsvdt_synchronize(self._h))

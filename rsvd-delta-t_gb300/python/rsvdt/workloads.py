@@ -1,0 +1,125 @@
+"""Benchmark workloads and their algorithmic byte counts.
+
+3D64: the five-field synthetic LNS-like operator on a 64^3 grid
+(N = 5*64^3 = 1,310,720; 1,810,432 dense 5x5 complex128 blocks, about
+45.26M nonzeros), k = 10 test vectors, Nw = 32 frequencies, q = 1, diagonal
+W_q = W_f from cell volumes in [0.5, 1.5]. Choices the configuration leaves
+open and that are fixed here: base frequency w0 = 0.1 (T = 2 pi / w0),
+domain x in [0, 10) streamwise and y, z in [-5, 5] (jet radius 1), dt from
+the RK4 stability limit 2.5 / rho with rho a Gershgorin bound on |lambda|,
+two transient periods, spectral shift placing the rightmost eigenvalue of
+the local 5x5 centre blocks at -0.05.
+
+GL1: the 500-node Ginzburg-Landau operator, k = 10, Nw = 64, dt = T/4096,
+one transient period.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import synth
+
+
+@dataclass
+class Workload:
+    name: str
+    N: int
+    k: int
+    Nw: int
+    q: int
+    w: float
+    dt_in: float
+    transient_length: float
+    transient_removal: bool
+    bcsr: tuple | None = None
+    csr: object | None = None
+    weights: dict = field(default_factory=dict)
+    meta: dict = field(default_factory=dict)
+
+    def params(self, **kw):
+        from . import default_params
+        return default_params(k=self.k, q=self.q, Nw=self.Nw, w=self.w, dt=self.dt_in,
+                              TransientLength=self.transient_length,
+                              TransientRemoval=int(self.transient_removal), Display=0, **kw)
+
+    def operator_bytes(self, s_c: int = 16) -> int:
+        """S_A: bytes of A (or A^H) read once: values + indices."""
+        if self.bcsr is not None:
+            br, bc, bl = self.bcsr
+            nblk, bs = bl.shape[0], bl.shape[1]
+            return nblk * bs * bs * s_c + nblk * 4 + (br.size) * 4
+        A = self.csr
+        return A.nnz * s_c + A.nnz * 4 + (A.shape[0] + 1) * 4
+
+    def step_bytes(self, R: int, s_c: int = 16) -> dict:
+        """Algorithmic bytes of one forced RK4 step over all k test vectors:
+        B_step = 4 S_A + S_F + 19 S_v + S_v / R with S_F = N Nw k s_c (the
+        forcing coefficients read once per step for both forcing times),
+        S_v = N k s_c (one state-sized vector pass), 19 vector passes
+        (stage inputs formed from y and the previous stage, forcing written
+        once and read by the stages that add it), one ring sample every R
+        steps. Stage 1 alone: S_A + S_F + 5 S_v."""
+        S_A = self.operator_bytes(s_c)
+        S_F = self.N * self.Nw * self.k * s_c
+        S_v = self.N * self.k * s_c
+        return dict(S_A=S_A, S_F=S_F, S_v=S_v, step=4 * S_A + S_F + 19 * S_v + S_v / R,
+                    stage1=S_A + S_F + 5 * S_v)
+
+    def step_flops(self) -> dict:
+        """Arithmetic of one step: 8 flops per complex multiply-add (4 FMA)."""
+        nnz = self.csr.nnz if self.csr is not None else self.bcsr[2].size
+        spmm = 4 * nnz * self.k
+        forcing = 2 * self.N * self.Nw * self.k
+        return dict(step=8.0 * (spmm + forcing), stage1=8.0 * (nnz * self.k + forcing))
+
+
+def gershgorin_bound_bcsr(browptr, bcol, blocks) -> float:
+    """max_i sum_j |a_ij| over the rows of a block-CSR matrix."""
+    nb = browptr.size - 1
+    rowsum = np.abs(blocks).sum(axis=2)  # (nblk, bs)
+    rows_of_block = np.repeat(np.arange(nb), np.diff(browptr))
+    acc = np.zeros((nb, blocks.shape[1]))
+    np.add.at(acc, rows_of_block, rowsum)
+    return float(acc.max())
+
+
+def local_shift(browptr, bcol, blocks, target: float = -0.05) -> float:
+    """Shift s such that the rightmost eigenvalue over all centre 5x5 blocks
+    of A - s I is `target`."""
+    nb = browptr.size - 1
+    rows_of_block = np.repeat(np.arange(nb), np.diff(browptr))
+    center = blocks[bcol == rows_of_block]
+    ev = np.linalg.eigvals(center)
+    return float(ev.real.max() - target)
+
+
+def make_3d(n: int = 64, k: int = 10, Nw: int = 32, q: int = 1, seed: int = 7, w: float = 0.1,
+            periods: float = 2.0, with_weights: bool = True) -> Workload:
+    br, bc, bl = synth.op3d_blocks(n=n, seed=seed, shift=0.0)
+    s = local_shift(br, bc, bl)
+    nb = br.size - 1
+    rows_of_block = np.repeat(np.arange(nb), np.diff(br))
+    cidx = np.nonzero(bc == rows_of_block)[0]
+    eye = np.arange(bl.shape[1])
+    bl[cidx[:, None], eye[None, :], eye[None, :]] -= s
+    rho = gershgorin_bound_bcsr(br, bc, bl)
+    dt_in = 2.5 / rho
+    T = 2 * math.pi / w
+    N = nb * bl.shape[1]
+    wl = Workload(name=f"3D{n}", N=N, k=k, Nw=Nw, q=q, w=w, dt_in=dt_in,
+                  transient_length=periods * T, transient_removal=False, bcsr=(br, bc, bl),
+                  meta=dict(shift=s, gershgorin=rho, seed=seed, grid=f"{n}^3", blocks=int(bl.shape[0]),
+                            nnz=int(bl.size)))
+    if with_weights:
+        wl.weights = dict(zip(("W_sqrt", "W_sqrt_inv"), synth.diag_weights(N, seed=seed + 4)))
+    return wl
+
+
+def make_gl1(k: int = 10, q: int = 1, transient_removal: bool = False) -> Workload:
+    A = synth.gl_operator(500)
+    dt, T = synth.gl_time_grid(0.1, 4096)
+    return Workload(name="GL1", N=500, k=k, Nw=64, q=q, w=0.1, dt_in=dt, transient_length=T,
+                    transient_removal=transient_removal, csr=A)

@@ -1,0 +1,80 @@
+"""CPU checks of the C ABI library: it builds, loads, and exports every
+function include/rsvdt.h declares; without a GPU, creating a context fails
+cleanly with RSVDT_ERR_CUDA (no CPU fallback). No compute calls."""
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "rsvdt.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(rsvdt_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_documented_entry_points():
+    names = declared_functions()
+    for must in ["rsvdt_create", "rsvdt_set_operator", "rsvdt_set_weight", "rsvdt_set_sketch", "rsvdt_action",
+                 "rsvdt_qr_all_freqs", "rsvdt_svd_all_freqs", "rsvdt_run", "rsvdt_get_results",
+                 "rsvdt_last_error", "rsvdt_destroy"]:
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    import ctypes
+
+    lib = ctypes.CDLL(built_lib)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_the_header(built_lib):
+    import rsvdt
+
+    assert sorted(rsvdt.EXPORTED) == declared_functions()
+    rsvdt.load_library()
+
+
+def test_params_defaults_follow_the_reference(built_lib):
+    # SourceCode/ReadUserInput.c:109-130: k = 3, q = 0, Display = 2.
+    import rsvdt
+
+    p = rsvdt.default_params()
+    assert (p.k, p.q, p.Display, p.precision) == (3, 0, 2, 0)
+
+
+def test_struct_layout_matches_the_header(built_lib):
+    import ctypes
+
+    import rsvdt
+
+    # int64 x3, double, int32 (+pad), double x2, int32 x2, double, int32 x2
+    assert ctypes.sizeof(rsvdt.Params) == 80
+    assert ctypes.sizeof(rsvdt.Grid) == 72
+
+
+def test_create_without_gpu_fails_cleanly(built_lib):
+    import torch
+
+    import rsvdt
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(rsvdt.RsvdtError) as e:
+        rsvdt.Context(rsvdt.default_params(k=2, Nw=8, w=0.1, dt=0.1, TransientLength=1.0))
+    assert e.value.status == rsvdt.ERR_CUDA
+
+
+def test_invalid_params_are_rejected_before_the_device(built_lib):
+    import rsvdt
+
+    for bad in [dict(k=0), dict(Nw=0), dict(w=0.0), dict(dt=-1.0), dict(DiscFlg=1, beta=-0.5)]:
+        kw = dict(k=2, Nw=8, w=0.1, dt=0.1, TransientLength=1.0)
+        kw.update(bad)
+        with pytest.raises(rsvdt.RsvdtError) as e:
+            rsvdt.Context(rsvdt.default_params(**kw))
+        assert e.value.status == rsvdt.ERR_ARG, bad

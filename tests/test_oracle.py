@@ -1,0 +1,146 @@
+"""The CPU oracle against closed forms, the dense FP64 resolvent and the
+reference's tutorial known answer (tests/golden/, made by make_golden.py)."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from rsvdt import petsc_io, synth
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_time_grid_follows_setup_time_freq_grid():
+    # SourceCode/SetupTimeFreqGrid.c:16-21 on the two configurations used.
+    dt, T = synth.gl_time_grid(0.1, 4096)
+    assert oracle.setup_grid(0.1, 64, dt, T)[1:] == (4096, 4096, 64)
+    d, Ns, Nt, R = oracle.setup_grid(0.05, 42, 0.003, 10.0)
+    T = 2 * math.pi / 0.05
+    assert Ns == 42 * math.ceil((T / 42) / 0.003)
+    assert (Ns, Nt, R) == (41916, 3336, 998)
+    assert abs(d - (T / 42) / math.ceil((T / 42) / 0.003)) < 1e-18
+
+
+@pytest.mark.parametrize("Nw", [8, 7, 16])
+def test_idft_and_dft_tables(Nw):
+    """idft[iw, jt] = exp(+2 pi i f jt / (2 Ns)) / Ns with f = iw for the
+    first half and iw - Nw for the rest (SourceCode/CreateDFTiDFTMats.c:42-59),
+    dft[j, iw] = exp(-2 pi i j iw / Nw) (:61-85)."""
+    Ns = 5 * Nw
+    idft = np.zeros(2 * Nw * 2 * Ns)
+    oracle.lib().orc_build_idft(Nw, Ns, 0, oracle._d(idft))
+    idft = idft.view(complex).reshape(Nw, 2 * Ns)
+    half = Nw // 2 - 1 if Nw % 2 == 0 else (Nw - 1) // 2
+    f = np.array([i if i <= half else i - Nw for i in range(Nw)])
+    jt = np.arange(2 * Ns)
+    ref = np.exp(2j * np.pi * np.outer(f, jt) / (2 * Ns)) / Ns
+    assert np.abs(idft - ref).max() < 1e-13
+    dft = np.zeros(2 * Nw * Nw)
+    oracle.lib().orc_build_dft(Nw, Nw, 0, oracle._d(dft))
+    dft = dft.view(complex).reshape(Nw, Nw)  # [iw][j]
+    j = np.arange(Nw)
+    assert np.abs(dft - np.exp(-2j * np.pi * np.outer(np.arange(Nw), j) / Nw)).max() < 1e-13
+
+
+def _small():
+    A = synth.gl_operator(64, mu0=0.2)
+    w, Nw = 0.1, 16
+    return A, w, Nw, 0.15, 2 * np.pi / w
+
+
+def test_direct_action_is_the_resolvent_up_to_a_phase():
+    """Y[:, iw] = e^{i w (Nt+R) dt} R(w) F[:, iw] to RK4 / transient accuracy
+    with transient removal (the reference's phase convention)."""
+    A, w, Nw, dt, T = _small()
+    o = oracle.Oracle(A, Nw, w, dt, T, transient_removal=True)
+    F = synth.complex_normal(64, Nw, 3)
+    Y = o.ts_action(1, F)
+    Ad = A.toarray()
+    for iw in range(Nw):
+        om = oracle.freq_of(iw, Nw, w)
+        x = np.linalg.solve(1j * om * np.eye(64) - Ad, F[:, iw])
+        ph = np.exp(1j * om * (o.Nt + o.R) * o.dt)
+        assert np.linalg.norm(Y[:, iw] - ph * x) / np.linalg.norm(x) < 1e-4
+
+
+def test_adjoint_action_is_the_adjoint_resolvent_up_to_a_phase():
+    A, w, Nw, dt, T = _small()
+    o = oracle.Oracle(A, Nw, w, dt, T, transient_removal=True)
+    F = synth.complex_normal(64, Nw, 4)
+    Y = o.ts_action(0, F)
+    Ad = A.toarray()
+    for iw in range(Nw):
+        om = oracle.freq_of(iw, Nw, w)
+        x = np.linalg.solve((1j * om * np.eye(64) - Ad).conj().T, F[:, iw])
+        c = np.vdot(x, Y[:, iw]) / np.vdot(x, x)
+        assert abs(abs(c) - 1) < 1e-4
+        assert np.linalg.norm(Y[:, iw] - c * x) / np.linalg.norm(x) < 1e-4
+
+
+def test_rsvd_gains_match_the_dense_resolvent():
+    A, w, Nw, dt, T = _small()
+    o = oracle.Oracle(A, Nw, w, dt, T, transient_removal=True)
+    k = 4
+    F = synth.complex_normal(64, k * Nw, 5)
+    _, _, S = o.run(F, 1)
+    om = [oracle.freq_of(i, Nw, w) for i in range(Nw)]
+    Sd, _, _ = oracle.dense_resolvent_svd(A, om, k)
+    gap = Sd[0] / Sd[1]
+    good = gap > 3
+    assert good.sum() >= 4
+    # RK4 truncation error at |lambda| dt ~ 1.8 bounds the agreement here.
+    assert (np.abs(S[0, good] - Sd[0, good]) / Sd[0, good]).max() < 1e-3
+
+
+def test_qr_and_svd_helpers():
+    Y = synth.complex_normal(50, 12, 6)
+    Q = oracle.qr_all_freqs(Y, 4)
+    for iw in range(3):
+        b = Q[:, iw * 4:(iw + 1) * 4]
+        assert np.abs(b.conj().T @ b - np.eye(4)).max() < 1e-14
+        R = b.conj().T @ Y[:, iw * 4:(iw + 1) * 4]
+        assert np.allclose(np.tril(R, -1), 0, atol=1e-12)
+        assert (np.diag(R).real > 0).all() and np.abs(np.diag(R).imag).max() < 1e-12
+    U, S = oracle.svd_all_freqs(Y, 4)
+    for iw in range(3):
+        s = np.linalg.svd(Y[:, iw * 4:(iw + 1) * 4], compute_uv=False)
+        assert np.abs(S[:, iw] - s).max() / s[0] < 1e-14
+
+
+def test_golden_tutorial_known_answer():
+    """The reference's own known answer (Tutorial/Ginzburg-Landau: sigma_1
+    peaks near 1.6e3 at omega = -0.65, gains.png) holds for the dense
+    resolvent of the shipped operator and for the oracle's RSVD-dt run of the
+    full tutorial configuration stored in the fixture."""
+    g = json.load(open(os.path.join(GOLDEN, "gl_tutorial.json")))
+    om = np.array(g["omega"])
+    Sd = np.array(g["dense_gains"])
+    So = np.array(g["oracle_gains"])
+    ka = g["known_answer"]
+    iw = int(np.argmax(Sd[0]))
+    assert abs(om[iw] - ka["omega_peak"]) < 1e-12
+    assert abs(Sd[0, iw] - ka["sigma1_peak"]) / ka["sigma1_peak"] < 0.06
+    assert int(np.argmax(So[0])) == iw
+    assert abs(So[0, iw] - Sd[0, iw]) / Sd[0, iw] < 1e-6
+    # Leading gains of the RSVD-dt run against the dense oracle wherever the
+    # singular-value gap lets k=10, q=1 converge.
+    good = Sd[0] / Sd[1] > 2
+    assert (np.abs(So[0, good] - Sd[0, good]) / Sd[0, good]).max() < 1e-3
+    assert g["grid"] == {"dt": g["grid"]["dt"], "Ns": 41916, "Nt": 3336, "ResRatio": 998}
+
+
+@pytest.mark.slow
+def test_oracle_reproduces_the_tutorial_peak():
+    """Re-runs the oracle on the shipped A_GL (k=2, q=0, transient removal)
+    and recovers the published peak gain at omega = -0.65."""
+    A = petsc_io.read_mat(os.path.join(GOLDEN, "A_GL"))
+    o = oracle.Oracle(A, 42, 0.05, 0.003, 10.0, transient_removal=True)
+    F = synth.gl_sketch(500, 2, 42, seed=14)
+    _, _, S = o.run(F, 0)
+    g = json.load(open(os.path.join(GOLDEN, "gl_tutorial.json")))
+    Sd = np.array(g["dense_gains"])
+    iw = int(np.argmax(Sd[0]))
+    assert abs(S[0, iw] - Sd[0, iw]) / Sd[0, iw] < 1e-4
