@@ -193,6 +193,32 @@ rsvdt_status rsvdt_rk4_advance(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_
 rsvdt_status rsvdt_rk4_profile(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps,
                                double *stage_ms);
 
+/* QR of every frequency block without allocating device memory.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc (work issued while another stream is being captured into a
+ * CUDA graph, host frameworks whose pool owns all device memory, services
+ * that forbid allocation after start-up). It needs no context.
+ *
+ * Y (input) and Q (output) are caller-allocated device arrays of rows x nw
+ * x k complex128 values in the library's spectral-block layout
+ * Y[(row*nw + iw)*k + j]; Q may equal Y. Each row-frequency block is
+ * orthonormalised with the same shifted CholQR passes as
+ * rsvdt_qr_all_freqs, on `stream` (a cudaStream_t; NULL is the legacy
+ * default stream), and the call returns after the stream has finished
+ * this work.
+ *
+ * Scratch comes from a fixed 4 MiB device array inside the library, one
+ * per GPU that loads it, held until the process exits. Limits: k <= 32 and
+ * nw*k*k <= 65535; larger sizes return RSVDT_ERR_ARG without touching the
+ * GPU. The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call reuses the same array, so calls that overlap on the GPU (from
+ * two streams or two host threads at once) race and must be serialised by
+ * the caller. errbuf (optional, errlen bytes) receives a message on
+ * failure. */
+rsvdt_status rsvdt_qr_all_freqs_noalloc(const double *Y, double *Q, int64_t rows, int64_t nw,
+                                        int64_t k, void *stream, char *errbuf, int64_t errlen);
+
 /* Waits for the context's stream. */
 rsvdt_status rsvdt_synchronize(rsvdt_ctx *ctx);
 

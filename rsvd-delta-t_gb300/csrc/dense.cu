@@ -750,3 +750,145 @@ rsvdt_status transient_removal(rsvdt_ctx *ctx, int dir, int prec, z128 *out) {
 
 }  // namespace rsvdt
 
+// ------------------------------------- QR without any device allocation
+//
+// rsvdt_qr_all_freqs_noalloc orthonormalises caller-owned device blocks
+// with the same CholQR passes as QRAllFreqs, but takes its scratch (Gram
+// partials, Gram matrices, R^{-1}, a status flag) from the file-scope
+// device array below instead of allocating. It is meant for callers that
+// cannot call cudaMalloc: code running while a stream capture is open
+// elsewhere, host frameworks that own all device memory through their own
+// pool (a PETSc/SLEPc application with its own allocator, for example), or
+// long-running services that forbid allocation after start-up. The array
+// is fixed at kNoAllocScratchBytes per device that loads this library and
+// stays resident until the process exits.
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 4u << 20;  // 4 MiB
+constexpr size_t kNoAllocElems = kNoAllocScratchBytes / sizeof(rsvdt::z128);
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) rsvdt::z128 g_noalloc_scratch[kNoAllocElems];
+
+// Device address of g_noalloc_scratch, looked up once per device.
+static void *g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+
+// Gram partials with a caller-chosen chunk length (variant of k_gram_part,
+// which uses a fixed chunk of kGramRows rows).
+__global__ void __launch_bounds__(256) k_gram_part_chunk(const rsvdt::z128 *__restrict__ X, int64_t sx,
+                                                         int64_t rows, int K, int64_t chunk_rows,
+                                                         rsvdt::z128 *__restrict__ part) {
+  using namespace rsvdt;
+  extern __shared__ z128 sm[];  // [kGramTile][K]
+  const int iw = blockIdx.y, nw = gridDim.y;
+  const int64_t n0 = (int64_t)blockIdx.x * chunk_rows;
+  const int64_t n1 = min(rows, n0 + chunk_rows);
+  const int pairs = K * K;
+  const int pbase = blockIdx.z * 1024;
+  z128 acc[4];
+  for (int q = 0; q < 4; ++q) acc[q] = zmake<z128>(0, 0);
+  for (int64_t nb = n0; nb < n1; nb += kGramTile) {
+    const int nr = (int)min((int64_t)kGramTile, n1 - nb);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nr * K; e += blockDim.x) {
+      int rr = e / K, a = e - rr * K;
+      sm[rr * K + a] = X[(nb + rr) * sx + (int64_t)iw * K + a];
+    }
+    __syncthreads();
+    for (int q = 0; q < 4; ++q) {
+      const int p = pbase + threadIdx.x + q * blockDim.x;
+      if (p >= pairs) break;
+      const int a = p / K, b = p - a * K;
+      z128 s = acc[q];
+      for (int rr = 0; rr < nr; ++rr) zmacc(s, sm[rr * K + a], sm[rr * K + b]);
+      acc[q] = s;
+    }
+  }
+  for (int q = 0; q < 4; ++q) {
+    const int p = pbase + threadIdx.x + q * blockDim.x;
+    if (p >= pairs) break;
+    part[((int64_t)blockIdx.x * nw + iw) * pairs + p] = acc[q];
+  }
+}
+
+static rsvdt_status noalloc_fail(char *errbuf, int64_t errlen, rsvdt_status st, const char *fmt, ...) {
+  if (errbuf && errlen > 0) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(errbuf, (size_t)errlen, fmt, ap);
+    va_end(ap);
+  }
+  return st;
+}
+
+}  // namespace
+
+extern "C" rsvdt_status rsvdt_qr_all_freqs_noalloc(const double *Y, double *Q, int64_t rows, int64_t nw,
+                                                   int64_t k, void *stream, char *errbuf, int64_t errlen) {
+  using namespace rsvdt;
+  if (errbuf && errlen > 0) errbuf[0] = '\0';
+  if (!Y || !Q || rows < 1 || nw < 1 || k < 1)
+    return noalloc_fail(errbuf, errlen, RSVDT_ERR_ARG, "invalid arguments (null pointer or non-positive size)");
+  if (k > 32 || rows > INT32_MAX)
+    return noalloc_fail(errbuf, errlen, RSVDT_ERR_ARG, "k = %lld exceeds 32 or rows exceed 2^31",
+                        (long long)k);
+  // Scratch layout (complex values): partials [chunks][nw][k][k], G, Rinv,
+  // R [nw][k][k] each, then one element holding the status flag.
+  const int64_t pk = nw * k * k;
+  const int64_t avail = (int64_t)kNoAllocElems - 1;
+  if (4 * pk > avail)
+    return noalloc_fail(errbuf, errlen, RSVDT_ERR_ARG,
+                        "nw*k*k = %lld needs %lld bytes of scratch; the fixed scratch array holds %zu bytes "
+                        "(limit nw*k*k <= %lld)",
+                        (long long)pk, (long long)(4 * pk + 1) * 16, kNoAllocScratchBytes, (long long)(avail / 4));
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
+    return noalloc_fail(errbuf, errlen, RSVDT_ERR_CUDA, "no usable current CUDA device (%s)", cudaGetErrorString(e));
+  if (!g_noalloc_ptr[dev]) {
+    // First call on this device: look up the array's device address (a host
+    // symbol's address is not a device address).
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return noalloc_fail(errbuf, errlen, RSVDT_ERR_CUDA, "cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = p;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  z128 *scr = (z128 *)g_noalloc_ptr[dev];
+  int64_t chunks = std::min((rows + kGramRows - 1) / kGramRows, avail / pk - 3);
+  if (chunks < 1) chunks = 1;
+  const int64_t chunk_rows = (rows + chunks - 1) / chunks;
+  chunks = (rows + chunk_rows - 1) / chunk_rows;
+  z128 *part = scr, *G = scr + chunks * pk, *R = G + pk, *Rinv = R + pk;
+  int32_t *flag = (int32_t *)(scr + avail);
+  z128 *out = (z128 *)Q;
+  if (Q != Y) {
+    e = cudaMemcpyAsync(Q, Y, sizeof(z128) * rows * nw * k, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return noalloc_fail(errbuf, errlen, RSVDT_ERR_CUDA, "copy: %s", cudaGetErrorString(e));
+  }
+  // The flag keeps the previous call's value: clear it.
+  e = cudaMemsetAsync(flag, 0, sizeof(int32_t), s);
+  if (e != cudaSuccess) return noalloc_fail(errbuf, errlen, RSVDT_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+  const int K = (int)k;
+  const int per = 256 / K;
+  for (int p = 0; p < 3; ++p) {  // one shifted pass, two plain (as rsvdt_qr_all_freqs)
+    const double shift = p < 1 ? 11.0 * ((double)rows * k + (double)k * (k + 1)) * 1.1102230246251565e-16 : 0.0;
+    dim3 g((unsigned)chunks, (unsigned)nw, (unsigned)((K * K + 1023) / 1024));
+    k_gram_part_chunk<<<g, 256, sizeof(z128) * kGramTile * K, s>>>(out, nw * k, rows, K, chunk_rows, part);
+    k_gram_reduce<<<grid_for(pk, 256), 256, 0, s>>>(part, (int)chunks, (int)nw, K * K, G);
+    k_chol<<<grid_for(nw, 64), 64, 0, s>>>(G, (int)nw, K, shift, R, Rinv, nullptr, flag);
+    k_apply_small<<<grid_for(rows * nw, per), per * K, sizeof(z128) * per * K, s>>>(out, nw * k, rows, (int)nw, K,
+                                                                                     Rinv, 1);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return noalloc_fail(errbuf, errlen, RSVDT_ERR_CUDA, "launch: %s", cudaGetErrorString(e));
+  int32_t hflag = 0;
+  e = cudaMemcpyAsync(&hflag, flag, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return noalloc_fail(errbuf, errlen, RSVDT_ERR_CUDA, "sync: %s", cudaGetErrorString(e));
+  if (hflag & 2)
+    return noalloc_fail(errbuf, errlen, RSVDT_ERR_NOT_SPD, "Cholesky of a Gram matrix failed: a block is rank deficient");
+  return RSVDT_OK;
+}

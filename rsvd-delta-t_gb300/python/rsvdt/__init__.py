@@ -38,7 +38,21 @@ EXPORTED = [
     "rsvdt_qr_all_freqs", "rsvdt_svd_all_freqs", "rsvdt_power_iteration", "rsvdt_run",
     "rsvdt_get_results", "rsvdt_rk4_steps", "rsvdt_rk4_reset", "rsvdt_rk4_advance",
     "rsvdt_rk4_profile", "rsvdt_synchronize", "rsvdt_stream", "rsvdt_launch_count",
+    "rsvdt_qr_all_freqs_noalloc",
 ]
+
+
+def qr_all_freqs_noalloc(Y_dev: int, Q_dev: int, rows: int, nw: int, k: int, stream: int = 0) -> None:
+    """Binding of rsvdt_qr_all_freqs_noalloc: orthonormalises each
+    frequency block of a caller-allocated device array (device pointers as
+    integers, layout [row][iw][k] complex128) without allocating any device
+    memory. Raises RsvdtError with the library's message on failure."""
+    lib = load_library()
+    buf = C.create_string_buffer(512)
+    st = lib.rsvdt_qr_all_freqs_noalloc(C.c_void_p(Y_dev), C.c_void_p(Q_dev), rows, nw, k,
+                                        C.c_void_p(stream) if stream else None, buf, len(buf))
+    if st != OK:
+        raise RsvdtError(st, buf.value.decode())
 
 
 class Params(C.Structure):
@@ -102,6 +116,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "rsvdt_rk4_reset": (C.c_int, [vp, C.c_int]),
         "rsvdt_rk4_advance": (C.c_int, [vp, C.c_int, i64, i64]),
         "rsvdt_rk4_profile": (C.c_int, [vp, C.c_int, i64, i64, d]),
+        "rsvdt_qr_all_freqs_noalloc": (C.c_int, [vp, vp, i64, i64, i64, vp, C.c_char_p, i64]),
         "rsvdt_synchronize": (C.c_int, [vp]),
         "rsvdt_stream": (vp, [vp]),
         "rsvdt_launch_count": (i64, [vp]),
