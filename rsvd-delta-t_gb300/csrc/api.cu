@@ -189,6 +189,7 @@ static rsvdt_status setup_grid_and_tables(rsvdt_ctx *ctx) {
   ctx->Nw = p.Nw;
   ctx->R = ctx->Ns / p.Nw;
   ctx->Nw_eff = ctx->real_op ? p.Nw / 2 : p.Nw;  // SourceCode/LNSStructure.c:44
+  ctx->pair = !ctx->real_op && ctx->Nw_eff % 2 == 0;
   if (ctx->R < 1 || ctx->Nw_eff < 1)
     return set_err(ctx, RSVDT_ERR_ARG, "time grid is degenerate (Ns=%lld, Nw=%lld)", (long long)ctx->Ns,
                    (long long)p.Nw);
@@ -327,17 +328,10 @@ static rsvdt_status weight_step(rsvdt_ctx *ctx, const DevCSR &M, int64_t rows_in
   return RSVDT_OK;
 }
 
-// Copies the working block (N rows) into the forcing-coefficient buffer in
-// the action's precision (TSActionRK4 copies Y_hat to F_hat,
+// Stages the working block (N rows) as the action's forcing slabs in the
+// action's precision (TSActionRK4 copies Y_hat to F_hat,
 // SourceCode/TSActionRK4.c:49).
-static rsvdt_status stage_forcing(rsvdt_ctx *ctx, int prec) {
-  const int64_t n = ctx->N * ctx->Nw_eff * ctx->K;
-  if (prec == RSVDT_PREC_C64) return launch_convert_to64(ctx, ctx->blk, (z64 *)ctx->Fh, n);
-  return cuda_ok(ctx, cudaMemcpyAsync(ctx->Fh, ctx->blk, sizeof(z128) * n, cudaMemcpyDeviceToDevice, ctx->stream),
-                 "copy")
-             ? RSVDT_OK
-             : RSVDT_ERR_CUDA;
-}
+static rsvdt_status stage_forcing(rsvdt_ctx *ctx, int prec) { return stage_forcing_coeffs(ctx, prec); }
 
 static rsvdt_status require_ready(rsvdt_ctx *ctx, bool need_block) {
   if (!ctx) return RSVDT_ERR_ARG;

@@ -116,6 +116,7 @@ struct rsvdt_ctx {
   int64_t Ns = 0, Nt = 0, R = 0, Nw = 0, Nw_eff = 0, K = 0;
   int64_t N = 0, Nb = 0, Nc = 0;
   bool real_op = false;
+  bool pair = false;  // forcing slabs hold +-f pairs (complex operator, even Nw)
   bool have_operator = false;
   bool have_block = false;
   bool have_results = false;
@@ -140,7 +141,8 @@ struct rsvdt_ctx {
   double *S = nullptr;  // [iw][k] gains
   size_t blk_elems = 0; // capacity of blk/blk2 in complex values
 
-  // Forcing coefficients of the running action, [n][iw][k].
+  // Forcing coefficients of the running action as frequency slabs
+  // [slab][n][k] (pair or plain, see step.cu).
   void *Fh = nullptr;
   // RK4 state, each N*K interleaved [n][k].
   void *y = nullptr, *zA = nullptr, *zB = nullptr, *acc = nullptr, *F2 = nullptr, *F3 = nullptr;
@@ -181,6 +183,7 @@ inline int grid_for(int64_t n, int threads) {
 
 // ------------------------------------------------- kernels (launchers)
 // step.cu
+rsvdt_status stage_forcing_coeffs(rsvdt_ctx *ctx, int prec);
 rsvdt_status launch_forcing_init(rsvdt_ctx *ctx, int dir, int prec);
 rsvdt_status run_steps(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_t nsteps,
                        bool sample);

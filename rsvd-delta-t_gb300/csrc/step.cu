@@ -11,11 +11,29 @@
 //   stage 3: k3 = A z' + F2;    z  = y + dt k3;    acc += (dt/6*2) k3
 //   stage 4: k4 = A z + F3;     y  = acc + dt/6 k4; sample y into the ring
 // acc accumulates the update in the reference's order (y += dt/6 k1;
-// y += dt/6*2 k2; ...). The forcing synthesis (SourceCode/CreateForcingOnFly.c)
-// reads each row's Fourier coefficients F_hat[n][iw][k] once per step for
-// both forcing times. The step index lives in device memory (two slots, so
+// y += dt/6*2 k2; ...). The step index lives in device memory (two slots, so
 // that no kernel reads the slot it writes), which lets a fixed CUDA graph of
 // G steps be replayed for the whole integration.
+//
+// Forcing synthesis (SourceCode/CreateForcingOnFly.c:17-19) reads the
+// running action's Fourier coefficients once per step for both forcing
+// times. They are staged per action as frequency slabs Fh[s][n][k], so that
+// a warp's loads are contiguous. For a complex operator with an even number
+// of frequencies the slabs hold symmetric pairs: slab 0 = c_0, slabs
+// 1..H-1 = c_f + c_{-f}, slabs H..2H-2 = i (c_f - c_{-f}), slab Nw-1 =
+// c_{-H} (H = Nw/2), since c_f e_f + c_{-f} conj(e_f) = (c_f + c_{-f}) Re e_f
+// + i (c_f - c_{-f}) Im e_f. A pair then costs two complex-by-real
+// multiply-adds instead of two complex ones: half the FP64 work of the
+// synthesis, the largest FP64 consumer after the sparse products. The
+// negative frequency's phasor is taken as the exact conjugate of the
+// positive one (the reference evaluates it from a much larger argument,
+// which carries its own rounding).
+//
+// Two kernel families: k_stage (one thread per row and test vector, any
+// CSR or block-CSR operator, any k) and k_bstage (one thread per row with
+// all k test vectors in registers, 5x5 block-CSR, k a compile-time
+// constant), which loads each operator entry once per row and every
+// k-vector row with 16-byte loads.
 #include <cstdarg>
 
 #include "common.cuh"
@@ -25,14 +43,14 @@ namespace rsvdt {
 template <class Z>
 struct StepArgs {
   int64_t N;
-  int K, Nw, dir;
+  int K, Nw, dir, pair;
   int64_t two_ns, R, Nt, Nstore;
   // Operator (A for the direct run, A^H for the adjoint run).
   const int32_t *__restrict__ rowptr;
   const int32_t *__restrict__ col;
   const Z *__restrict__ val;
-  int bs;  // 0: CSR; >0: block CSR with bs x bs blocks
-  const Z *__restrict__ Fh;   // [n][iw][k], nullptr when unforced
+  int bs;                     // 0: CSR; >0: block CSR with bs x bs blocks
+  const Z *__restrict__ Fh;   // [slab][n][k], nullptr when unforced
   const Z *__restrict__ tab;  // [2Ns][Nw]
   Z *y, *zA, *zB, *acc, *F2, *F3, *ring;
   typename real_of<Z>::type dt, dt_2, dt_6, dt_62;  // dt, dt/2, dt/6, dt/6*2
@@ -65,6 +83,34 @@ __device__ __forceinline__ int64_t ring_slot(int dir, int64_t i, int64_t Nt, int
   return pos % Nstore;
 }
 
+// Real weight of pair slab s (1 <= s <= 2H-2) at phasor row e.
+template <class Z>
+__device__ __forceinline__ typename real_of<Z>::type pair_weight(const Z *e, int s, int H) {
+  return s < H ? e[s].re : e[s - H + 1].im;
+}
+
+// Forcing at one time for one (row, test vector) from the slabs.
+template <class Z>
+__device__ __forceinline__ Z forcing_at(const StepArgs<Z> &P, int64_t n, int kc, const Z *e) {
+  Z f = zmake<Z>(0, 0);
+  const int64_t NK = P.N * P.K;
+  const Z *c = P.Fh + n * P.K + kc;
+  if (P.pair) {
+    const int H = P.Nw / 2;
+    zmac(f, c[0], e[0]);
+    for (int s = 1; s <= 2 * H - 2; ++s) {
+      const auto w = pair_weight(e, s, H);
+      const Z v = c[(int64_t)s * NK];
+      f.re = fma(w, v.re, f.re);
+      f.im = fma(w, v.im, f.im);
+    }
+    zmac(f, c[(int64_t)(P.Nw - 1) * NK], e[H]);
+  } else {
+    for (int s = 0; s < P.Nw; ++s) zmac(f, c[(int64_t)s * NK], e[s]);
+  }
+  return f;
+}
+
 // Sparse row product: acc += sum_j A[n,j] * x[j][kc].
 template <class Z>
 __device__ __forceinline__ void row_product(const StepArgs<Z> &P, int64_t n, int kc, const Z *x,
@@ -94,9 +140,10 @@ __device__ __forceinline__ void row_product(const StepArgs<Z> &P, int64_t n, int
   }
 }
 
+// ------------------------------------------------ generic stage kernels
+
 template <class Z, int S>
 __global__ void __launch_bounds__(256) k_stage(const StepArgs<Z> P) {
-  using Rl = typename real_of<Z>::type;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t NK = P.N * P.K;
   int64_t i = (S == 1) ? P.step[0] : P.step[1];
@@ -116,14 +163,8 @@ __global__ void __launch_bounds__(256) k_stage(const StepArgs<Z> P) {
     if (P.Fh) {
       int64_t j2, j3;
       step_idx(P.dir, i, P.two_ns, j2, j3);
-      const Z *e2 = P.tab + j2 * P.Nw;
-      const Z *e3 = P.tab + j3 * P.Nw;
-      const Z *c = P.Fh + n * (int64_t)P.Nw * P.K + kc;
-      for (int iw = 0; iw < P.Nw; ++iw) {
-        const Z cv = c[(int64_t)iw * P.K];
-        zmac(f2, cv, e2[iw]);
-        zmac(f3, cv, e3[iw]);
-      }
+      f2 = forcing_at(P, n, kc, P.tab + j2 * P.Nw);
+      f3 = forcing_at(P, n, kc, P.tab + j3 * P.Nw);
     }
     P.F2[t] = f2;
     P.F3[t] = f3;
@@ -142,7 +183,200 @@ __global__ void __launch_bounds__(256) k_stage(const StepArgs<Z> P) {
     if (p >= 0) P.ring[p * NK + t] = ynew;
     if (t == 0) P.step[0] = i + 1;
   }
-  (void)sizeof(Rl);
+}
+
+// --------------------------------- 5x5 block-CSR row kernels (k in registers)
+
+// Row of K complex values; 16-byte loads/stores (K even for complex64).
+template <class Z, int K>
+__device__ __forceinline__ void ld_row(const Z *p, Z (&v)[K]) {
+  if constexpr (sizeof(Z) == 8 && K % 2 == 0) {
+    const float4 *q = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+    for (int i = 0; i < K / 2; ++i) {
+      const float4 t = q[i];
+      v[2 * i] = zmake<Z>(t.x, t.y);
+      v[2 * i + 1] = zmake<Z>(t.z, t.w);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < K; ++i) v[i] = p[i];
+  }
+}
+
+// Read-only variant through the non-coherent path.
+template <class Z, int K>
+__device__ __forceinline__ void ldg_row(const Z *p, Z (&v)[K]) {
+  if constexpr (sizeof(Z) == 8 && K % 2 == 0) {
+    const float4 *q = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+    for (int i = 0; i < K / 2; ++i) {
+      const float4 t = __ldg(q + i);
+      v[2 * i] = zmake<Z>(t.x, t.y);
+      v[2 * i + 1] = zmake<Z>(t.z, t.w);
+    }
+  } else if constexpr (sizeof(Z) == 16) {
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      const double2 t = __ldg(q + i);
+      v[i] = zmake<Z>(t.x, t.y);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < K; ++i) v[i] = p[i];
+  }
+}
+
+template <class Z, int K>
+__device__ __forceinline__ void st_row(Z *p, const Z (&v)[K]) {
+  if constexpr (sizeof(Z) == 8 && K % 2 == 0) {
+    float4 *q = reinterpret_cast<float4 *>(p);
+#pragma unroll
+    for (int i = 0; i < K / 2; ++i) q[i] = make_float4(v[2 * i].re, v[2 * i].im, v[2 * i + 1].re, v[2 * i + 1].im);
+  } else {
+#pragma unroll
+    for (int i = 0; i < K; ++i) p[i] = v[i];
+  }
+}
+
+// Forcing at two times for one row, all K test vectors (pair or plain slabs);
+// e2 / e3 are the phasor rows staged in shared memory.
+template <class Z, int K>
+__device__ __forceinline__ void forcing_row(const StepArgs<Z> &P, int64_t n, const Z *e2, const Z *e3,
+                                            Z (&f2)[K], Z (&f3)[K]) {
+  const int64_t NK = P.N * K;
+  const Z *c = P.Fh + n * K;
+#pragma unroll
+  for (int q = 0; q < K; ++q) f2[q] = f3[q] = zmake<Z>(0, 0);
+  if (P.pair) {
+    const int H = P.Nw / 2;
+    Z v[K];
+    ldg_row<Z, K>(c, v);
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      zmac(f2[q], v[q], e2[0]);
+      zmac(f3[q], v[q], e3[0]);
+    }
+#pragma unroll 2
+    for (int s = 1; s <= 2 * H - 2; ++s) {
+      const auto w2 = pair_weight(e2, s, H), w3 = pair_weight(e3, s, H);
+      ldg_row<Z, K>(c + (int64_t)s * NK, v);
+#pragma unroll
+      for (int q = 0; q < K; ++q) {
+        f2[q].re = fma(w2, v[q].re, f2[q].re);
+        f2[q].im = fma(w2, v[q].im, f2[q].im);
+        f3[q].re = fma(w3, v[q].re, f3[q].re);
+        f3[q].im = fma(w3, v[q].im, f3[q].im);
+      }
+    }
+    ldg_row<Z, K>(c + (int64_t)(P.Nw - 1) * NK, v);
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      zmac(f2[q], v[q], e2[H]);
+      zmac(f3[q], v[q], e3[H]);
+    }
+  } else {
+#pragma unroll 2
+    for (int s = 0; s < P.Nw; ++s) {
+      Z v[K];
+      ldg_row<Z, K>(c + (int64_t)s * NK, v);
+#pragma unroll
+      for (int q = 0; q < K; ++q) {
+        zmac(f2[q], v[q], e2[s]);
+        zmac(f3[q], v[q], e3[s]);
+      }
+    }
+  }
+}
+
+static const int kRowThreads = 128;
+
+template <class Z, int K, int S>
+__global__ void __launch_bounds__(kRowThreads) k_bstage(const StepArgs<Z> P) {
+  extern __shared__ unsigned char smem_raw[];
+  Z *e2 = reinterpret_cast<Z *>(smem_raw);  // phasor rows of this step (stage 1)
+  Z *e3 = e2 + P.Nw;
+  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = (S == 1) ? P.step[0] : P.step[1];
+  if (S == 1) {
+    if (P.Fh) {
+      int64_t j2, j3;
+      step_idx(P.dir, i, P.two_ns, j2, j3);
+      for (int s = threadIdx.x; s < P.Nw; s += blockDim.x) {
+        e2[s] = P.tab[j2 * P.Nw + s];
+        e3[s] = P.tab[j3 * P.Nw + s];
+      }
+    }
+    __syncthreads();
+  }
+  if (n >= P.N) return;
+  if (S == 1 && n == 0) P.step[1] = i;
+  const Z *x = (S == 1) ? P.y : (S == 2) ? P.zA : (S == 3) ? P.zB : P.zA;
+  const Z *addv = (S == 1 || S == 4) ? P.F3 : P.F2;
+  Z k[K];
+  if (S == 1)
+    ld_row<Z, K>(addv + n * K, k);  // F3 is rewritten below by this thread
+  else
+    ldg_row<Z, K>(addv + n * K, k);
+  // Sparse product over the 5x5 blocks of block row n / 5.
+  {
+    const int64_t br = n / 5;
+    const int r = (int)(n - br * 5);
+    const int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
+    for (int32_t j = b; j < e; ++j) {
+      const int64_t c0 = (int64_t)__ldg(P.col + j) * 5;
+      const Z *arow = P.val + ((int64_t)j * 5 + r) * 5;
+      Z a[5];
+#pragma unroll
+      for (int c = 0; c < 5; ++c) a[c] = arow[c];
+#pragma unroll
+      for (int c = 0; c < 5; ++c) {
+        Z xv[K];
+        ldg_row<Z, K>(x + (c0 + c) * K, xv);
+#pragma unroll
+        for (int q = 0; q < K; ++q) zmac(k[q], a[c], xv[q]);
+      }
+    }
+  }
+  Z yv[K];
+  if (S != 4) ldg_row<Z, K>(P.y + n * K, yv);
+  if (S == 1) {
+    Z t[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) t[q] = zaxpy(P.dt_2, k[q], yv[q]);
+    st_row<Z, K>(P.zA + n * K, t);
+#pragma unroll
+    for (int q = 0; q < K; ++q) t[q] = zaxpy(P.dt_6, k[q], yv[q]);
+    st_row<Z, K>(P.acc + n * K, t);
+    Z f2[K], f3[K];
+    if (P.Fh) {
+      forcing_row<Z, K>(P, n, e2, e3, f2, f3);
+    } else {
+#pragma unroll
+      for (int q = 0; q < K; ++q) f2[q] = f3[q] = zmake<Z>(0, 0);
+    }
+    st_row<Z, K>(P.F2 + n * K, f2);
+    st_row<Z, K>(P.F3 + n * K, f3);
+  } else if (S == 2 || S == 3) {
+    Z t[K], av[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) t[q] = zaxpy(S == 2 ? P.dt_2 : P.dt, k[q], yv[q]);
+    st_row<Z, K>((S == 2 ? P.zB : P.zA) + n * K, t);
+    ld_row<Z, K>(P.acc + n * K, av);
+#pragma unroll
+    for (int q = 0; q < K; ++q) av[q] = zaxpy(P.dt_62, k[q], av[q]);
+    st_row<Z, K>(P.acc + n * K, av);
+  } else {
+    Z av[K];
+    ld_row<Z, K>(P.acc + n * K, av);
+#pragma unroll
+    for (int q = 0; q < K; ++q) av[q] = zaxpy(P.dt_6, k[q], av[q]);
+    st_row<Z, K>(P.y + n * K, av);
+    const int64_t p = P.ring ? ring_slot(P.dir, i, P.Nt, P.R, P.Nstore) : -1;
+    if (p >= 0) st_row<Z, K>(P.ring + (p * P.N + n) * K, av);
+    if (n == 0) P.step[0] = i + 1;
+  }
 }
 
 __global__ void k_set_step(int64_t *step, int64_t i) {
@@ -157,11 +391,42 @@ __global__ void k_forcing_init(const StepArgs<Z> P) {
   if (t >= P.N * P.K) return;
   const int64_t n = t / P.K;
   const int kc = (int)(t - n * P.K);
-  Z f = zmake<Z>(0, 0);
-  const Z *c = P.Fh + n * (int64_t)P.Nw * P.K + kc;
-  for (int iw = 0; iw < P.Nw; ++iw) zmac(f, c[(int64_t)iw * P.K], P.tab[iw]);
-  P.F3[t] = f;
+  P.F3[t] = forcing_at(P, n, kc, P.tab);
   P.y[t] = zmake<Z>(0, 0);
+}
+
+// Forcing slabs from the working block blk[n][iw][k] (complex128):
+// Fh[s][n][k], pair or plain (see the file comment), in precision Z.
+template <class Z>
+__global__ void k_stage_slabs(const z128 *__restrict__ blk, int64_t N, int Nw, int K, int pair,
+                              Z *__restrict__ Fh) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t NK = N * K;
+  if (u >= NK * Nw) return;
+  const int s = (int)(u / NK);
+  const int64_t r = u - (int64_t)s * NK;
+  const int64_t n = r / K;
+  const int kc = (int)(r - n * K);
+  const z128 *row = blk + n * (int64_t)Nw * K + kc;
+  z128 v;
+  if (!pair) {
+    v = row[(int64_t)s * K];
+  } else {
+    const int H = Nw / 2;
+    if (s == 0) {
+      v = row[0];
+    } else if (s == Nw - 1) {
+      v = row[(int64_t)H * K];
+    } else {
+      const int f = s < H ? s : s - H + 1;
+      const z128 cp = row[(int64_t)f * K], cn = row[(int64_t)(Nw - f) * K];
+      if (s < H)
+        v = zmake<z128>(cp.re + cn.re, cp.im + cn.im);
+      else  // i (cp - cn)
+        v = zmake<z128>(-(cp.im - cn.im), cp.re - cn.re);
+    }
+  }
+  Fh[u] = zmake<Z>((typename real_of<Z>::type)v.re, (typename real_of<Z>::type)v.im);
 }
 
 template <class Z>
@@ -170,6 +435,7 @@ static StepArgs<Z> make_args(rsvdt_ctx *ctx, int dir, bool forced) {
   P.N = ctx->N;
   P.K = (int)ctx->K;
   P.Nw = (int)ctx->Nw_eff;
+  P.pair = ctx->pair ? 1 : 0;
   P.dir = dir;
   P.two_ns = 2 * ctx->Ns;
   P.R = ctx->R;
@@ -208,14 +474,62 @@ static StepArgs<Z> make_args(rsvdt_ctx *ctx, int dir, bool forced) {
   return P;
 }
 
+// ---------------------------------------------------------- dispatch
+
+template <class Z, int K>
+static void launch_bstage(int stage, const StepArgs<Z> &P, cudaStream_t st) {
+  const int g = grid_for(P.N, kRowThreads);
+  const size_t sm = sizeof(Z) * 2 * (P.Nw > 0 ? P.Nw : 1);
+  switch (stage) {
+    case 1: k_bstage<Z, K, 1><<<g, kRowThreads, sm, st>>>(P); break;
+    case 2: k_bstage<Z, K, 2><<<g, kRowThreads, 0, st>>>(P); break;
+    case 3: k_bstage<Z, K, 3><<<g, kRowThreads, 0, st>>>(P); break;
+    default: k_bstage<Z, K, 4><<<g, kRowThreads, 0, st>>>(P); break;
+  }
+}
+
+// Launches stage `stage` (1..4) with the fastest kernel for the operator.
 template <class Z>
-static void enqueue_step(rsvdt_ctx *ctx, const StepArgs<Z> &P) {
+static void launch_stage(int stage, const StepArgs<Z> &P, cudaStream_t st) {
+  if (P.bs == 5) {
+    switch (P.K) {
+      case 2: return launch_bstage<Z, 2>(stage, P, st);
+      case 4: return launch_bstage<Z, 4>(stage, P, st);
+      case 6: return launch_bstage<Z, 6>(stage, P, st);
+      case 8: return launch_bstage<Z, 8>(stage, P, st);
+      case 10: return launch_bstage<Z, 10>(stage, P, st);
+      case 16: return launch_bstage<Z, 16>(stage, P, st);
+      default: break;
+    }
+  }
   const int th = 256;
   const int g = grid_for(P.N * P.K, th);
-  k_stage<Z, 1><<<g, th, 0, ctx->stream>>>(P);
-  k_stage<Z, 2><<<g, th, 0, ctx->stream>>>(P);
-  k_stage<Z, 3><<<g, th, 0, ctx->stream>>>(P);
-  k_stage<Z, 4><<<g, th, 0, ctx->stream>>>(P);
+  switch (stage) {
+    case 1: k_stage<Z, 1><<<g, th, 0, st>>>(P); break;
+    case 2: k_stage<Z, 2><<<g, th, 0, st>>>(P); break;
+    case 3: k_stage<Z, 3><<<g, th, 0, st>>>(P); break;
+    default: k_stage<Z, 4><<<g, th, 0, st>>>(P); break;
+  }
+}
+
+template <class Z>
+static void enqueue_step(rsvdt_ctx *ctx, const StepArgs<Z> &P) {
+  for (int s = 1; s <= 4; ++s) launch_stage(s, P, ctx->stream);
+}
+
+rsvdt_status stage_forcing_coeffs(rsvdt_ctx *ctx, int prec) {
+  const int64_t total = ctx->N * ctx->Nw_eff * ctx->K;
+  const int th = 256;
+  if (prec == RSVDT_PREC_C64)
+    k_stage_slabs<z64><<<grid_for(total, th), th, 0, ctx->stream>>>(ctx->blk, ctx->N, (int)ctx->Nw_eff,
+                                                                     (int)ctx->K, ctx->pair ? 1 : 0,
+                                                                     (z64 *)ctx->Fh);
+  else
+    k_stage_slabs<z128><<<grid_for(total, th), th, 0, ctx->stream>>>(ctx->blk, ctx->N, (int)ctx->Nw_eff,
+                                                                      (int)ctx->K, ctx->pair ? 1 : 0,
+                                                                      (z128 *)ctx->Fh);
+  ctx->launches += 1;
+  return cuda_ok(ctx, cudaGetLastError(), "forcing slabs") ? RSVDT_OK : RSVDT_ERR_CUDA;
 }
 
 rsvdt_status launch_forcing_init(rsvdt_ctx *ctx, int dir, int prec) {
@@ -274,8 +588,6 @@ template <class Z>
 static rsvdt_status profile_steps_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t nsteps,
                                     double *stage_ms) {
   auto P = make_args<Z>(ctx, dir, true);
-  const int th = 256;
-  const int g = grid_for(P.N * P.K, th);
   cudaEvent_t ev[5];
   for (auto &e : ev)
     if (!cuda_ok(ctx, cudaEventCreate(&e), "event create")) return RSVDT_ERR_CUDA;
@@ -285,14 +597,10 @@ static rsvdt_status profile_steps_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t
   rsvdt_status st = RSVDT_OK;
   for (int64_t n = 0; n < nsteps && st == RSVDT_OK; ++n) {
     cudaEventRecord(ev[0], ctx->stream);
-    k_stage<Z, 1><<<g, th, 0, ctx->stream>>>(P);
-    cudaEventRecord(ev[1], ctx->stream);
-    k_stage<Z, 2><<<g, th, 0, ctx->stream>>>(P);
-    cudaEventRecord(ev[2], ctx->stream);
-    k_stage<Z, 3><<<g, th, 0, ctx->stream>>>(P);
-    cudaEventRecord(ev[3], ctx->stream);
-    k_stage<Z, 4><<<g, th, 0, ctx->stream>>>(P);
-    cudaEventRecord(ev[4], ctx->stream);
+    for (int s = 1; s <= 4; ++s) {
+      launch_stage(s, P, ctx->stream);
+      cudaEventRecord(ev[s], ctx->stream);
+    }
     ctx->launches += 4;
     if (!cuda_ok(ctx, cudaEventSynchronize(ev[4]), "event sync")) {
       st = RSVDT_ERR_CUDA;

@@ -68,12 +68,20 @@ class Workload:
         return dict(S_A=S_A, S_F=S_F, S_v=S_v, step=4 * S_A + S_F + 19 * S_v + S_v / R,
                     stage1=S_A + S_F + 5 * S_v)
 
-    def step_flops(self) -> dict:
-        """Arithmetic of one step: 8 flops per complex multiply-add (4 FMA)."""
+    def step_flops(self, paired: bool = True) -> dict:
+        """Arithmetic of one step as executed: 8 flops per complex
+        multiply-add (4 FMA) in the sparse products; the forcing synthesis at
+        two times per step, with +-f frequency pairs (complex operator, even
+        Nw) costing 2 complex and Nw-2 complex-by-real multiply-adds (4 flops)
+        per time, otherwise Nw complex multiply-adds."""
         nnz = self.csr.nnz if self.csr is not None else self.bcsr[2].size
-        spmm = 4 * nnz * self.k
-        forcing = 2 * self.N * self.Nw * self.k
-        return dict(step=8.0 * (spmm + forcing), stage1=8.0 * (nnz * self.k + forcing))
+        spmm = 8.0 * nnz * self.k
+        if paired and self.Nw % 2 == 0:
+            per_time = 2 * 8.0 + (self.Nw - 2) * 4.0
+        else:
+            per_time = 8.0 * self.Nw
+        forcing = 2 * self.N * self.k * per_time
+        return dict(step=4 * spmm + forcing, stage1=spmm + forcing)
 
 
 def gershgorin_bound_bcsr(browptr, bcol, blocks) -> float:

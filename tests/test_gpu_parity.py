@@ -94,8 +94,12 @@ def test_rk4_steps_match_oracle(built_lib, direction):
     for ik in range(k):
         Fk = F[:, [iw * k + ik for iw in range(nwe)]]
         yo, F3o = orc.rk4_steps(direction, Fk, i0, 20, y0[:, ik], F30[:, ik])
-        assert rel(y[:, ik], yo) < 1e-13
-        assert rel(F3[:, ik], F3o) < 1e-13
+        # The GPU takes each negative frequency's phasor as the exact
+        # conjugate of the positive one; the reference evaluates it from an
+        # argument up to 2*pi*2Ns, which carries ~|arg| * 1.1e-16 of its own
+        # rounding (here < 1e-12).
+        assert rel(y[:, ik], yo) < 1e-11
+        assert rel(F3[:, ik], F3o) < 1e-11
     ctx.close()
 
 
@@ -114,8 +118,34 @@ def test_action_matches_oracle(built_lib, direction, tr):
     # Per frequency block relative error.
     for iw in range(g.Nw_eff):
         blk = slice(iw * k, (iw + 1) * k)
-        assert rel(Y[:, blk], Yo[:, blk]) < (1e-11 if not tr else 1e-9), iw
+        assert rel(Y[:, blk], Yo[:, blk]) < (1e-10 if not tr else 1e-9), iw
     ctx.close()
+
+
+@pytest.mark.parametrize("case", ["odd_nw", "real_operator"])
+def test_plain_forcing_paths_match_oracle(built_lib, case):
+    """Forcing without the +-f pairing: an odd number of frequencies, and a
+    real operator (positive frequencies only, Nw_eff = Nw/2,
+    SourceCode/LNSStructure.c:37-44)."""
+    if case == "odd_nw":
+        A, cfg = small_gl(Nw=15)
+    else:
+        A = synth.gl_operator(64, nu=2.0, gamma=1.0, mu0=0.2)  # real-valued
+        T = 2 * np.pi / 0.1
+        cfg = dict(w=0.1, Nw=16, dt=0.15, TransientLength=T)
+    k = 2
+    for direction in (1, 0):
+        ctx = make_ctx(A, cfg, k=k)
+        g = ctx.grid()
+        if case == "real_operator":
+            assert g.Nw_eff == 8
+        F = synth.complex_normal(A.shape[0], k * g.Nw_eff, 31)
+        ctx.set_sketch(F)
+        ctx.action(direction)
+        Y = ctx.get_block()
+        Yo = make_oracle(A, cfg).ts_action(direction, F)
+        assert rel(Y, Yo) < 1e-11
+        ctx.close()
 
 
 def test_qr_and_svd_match_oracle(built_lib):
