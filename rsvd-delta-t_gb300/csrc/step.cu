@@ -29,11 +29,13 @@
 // positive one (the reference evaluates it from a much larger argument,
 // which carries its own rounding).
 //
-// Two kernel families: k_stage (one thread per row and test vector, any
-// CSR or block-CSR operator, any k) and k_bstage (one thread per row with
-// all k test vectors in registers, 5x5 block-CSR, k a compile-time
-// constant), which loads each operator entry once per row and every
-// k-vector row with 16-byte loads.
+// Three kernel families: k_stage (one thread per row and test vector, any
+// CSR or block-CSR operator, any k); for 5x5 block-CSR with k a
+// compile-time constant, k_bstage (complex64: one lane per block row and
+// group of test vectors, which reads every gathered k-vector row as one
+// contiguous 16-byte-per-lane access, for HBM-bound stages) and k_rstage
+// (complex128: one thread per row with all k test vectors in registers,
+// full warps for the FP64-bound stages).
 #include <cstdarg>
 
 #include "common.cuh"
@@ -187,6 +189,218 @@ __global__ void __launch_bounds__(256) k_stage(const StepArgs<Z> P) {
 
 // --------------------------------- 5x5 block-CSR row kernels (k in registers)
 
+// KP consecutive complex values at a 16-byte aligned address.
+template <class Z, int KP>
+__device__ __forceinline__ void ld_chunk(const Z *p, Z (&v)[KP]) {
+  if constexpr (sizeof(Z) == 8 && KP == 2) {
+    const float4 t = *reinterpret_cast<const float4 *>(p);
+    v[0] = zmake<Z>(t.x, t.y);
+    v[1] = zmake<Z>(t.z, t.w);
+  } else {
+#pragma unroll
+    for (int i = 0; i < KP; ++i) v[i] = p[i];
+  }
+}
+
+template <class Z, int KP>
+__device__ __forceinline__ void ldg_chunk(const Z *p, Z (&v)[KP]) {
+  if constexpr (sizeof(Z) == 8 && KP == 2) {
+    const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+    v[0] = zmake<Z>(t.x, t.y);
+    v[1] = zmake<Z>(t.z, t.w);
+  } else if constexpr (sizeof(Z) == 16) {
+#pragma unroll
+    for (int i = 0; i < KP; ++i) {
+      const double2 t = __ldg(reinterpret_cast<const double2 *>(p) + i);
+      v[i] = zmake<Z>(t.x, t.y);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < KP; ++i) v[i] = p[i];
+  }
+}
+
+template <class Z, int KP>
+__device__ __forceinline__ void st_chunk(Z *p, const Z (&v)[KP]) {
+  if constexpr (sizeof(Z) == 8 && KP == 2) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0].re, v[0].im, v[1].re, v[1].im);
+  } else {
+#pragma unroll
+    for (int i = 0; i < KP; ++i) p[i] = v[i];
+  }
+}
+
+static const int kRowThreads = 128;
+
+// One lane per (5-row block row, group of KP test vectors). The L = K/KP
+// lanes of a block row fetch each gathered k-vector row together, one
+// 16-byte chunk each, so a row is one contiguous access instead of five
+// copies of it, and every lane keeps 5 x KP accumulators. Block rows are
+// packed 32/L to a warp. Vector rows (y, acc, the forcing slabs, ...) are
+// read and written the same way: the lanes of consecutive block rows cover
+// consecutive bytes.
+template <class Z, int K, int KP, int S>
+__global__ void __launch_bounds__(kRowThreads) k_bstage(const StepArgs<Z> P) {
+  constexpr int L = K / KP;
+  constexpr int BPW = 32 / L;
+  extern __shared__ unsigned char smem_raw[];
+  Z *e2 = reinterpret_cast<Z *>(smem_raw);  // phasor rows of this step (stage 1)
+  Z *e3 = e2 + P.Nw;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int sub = lane / L, q = lane - sub * L;
+  const int64_t br = warp * BPW + sub;
+  const int64_t i = (S == 1) ? P.step[0] : P.step[1];
+  if (S == 1) {
+    if (P.Fh) {
+      int64_t j2, j3;
+      step_idx(P.dir, i, P.two_ns, j2, j3);
+      for (int s = threadIdx.x; s < P.Nw; s += blockDim.x) {
+        e2[s] = P.tab[j2 * P.Nw + s];
+        e3[s] = P.tab[j3 * P.Nw + s];
+      }
+    }
+    __syncthreads();
+  }
+  if (sub >= BPW || br >= P.N / 5) return;
+  if (S == 1 && br == 0 && q == 0) P.step[1] = i;
+  const int64_t base = br * 5 * K + q * KP;  // element (row br*5, test vector q*KP)
+  const Z *x = (S == 1) ? P.y : (S == 2) ? P.zA : (S == 3) ? P.zB : P.zA;
+  const Z *addv = (S == 1 || S == 4) ? P.F3 : P.F2;
+  Z k[5][KP];
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    if (S == 1)
+      ld_chunk<Z, KP>(addv + base + r * K, k[r]);  // F3 is rewritten below by this lane
+    else
+      ldg_chunk<Z, KP>(addv + base + r * K, k[r]);
+  }
+  {
+    const int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
+    for (int32_t j = b; j < e; ++j) {
+      const int64_t c0 = (int64_t)__ldg(P.col + j) * 5;
+      const Z *blk = P.val + (int64_t)j * 25;
+#pragma unroll
+      for (int c = 0; c < 5; ++c) {
+        Z xv[KP];
+        ldg_chunk<Z, KP>(x + (c0 + c) * K + q * KP, xv);
+#pragma unroll
+        for (int r = 0; r < 5; ++r) {
+          const Z a = blk[r * 5 + c];
+#pragma unroll
+          for (int p = 0; p < KP; ++p) zmac(k[r][p], a, xv[p]);
+        }
+      }
+    }
+  }
+  if (S == 1) {
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      Z yv[KP], t[KP];
+      ldg_chunk<Z, KP>(P.y + base + r * K, yv);
+#pragma unroll
+      for (int p = 0; p < KP; ++p) t[p] = zaxpy(P.dt_2, k[r][p], yv[p]);
+      st_chunk<Z, KP>(P.zA + base + r * K, t);
+#pragma unroll
+      for (int p = 0; p < KP; ++p) t[p] = zaxpy(P.dt_6, k[r][p], yv[p]);
+      st_chunk<Z, KP>(P.acc + base + r * K, t);
+    }
+    // Forcing at the half step and the full step, pair or plain slabs.
+    Z f2[5][KP], f3[5][KP];
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int p = 0; p < KP; ++p) f2[r][p] = f3[r][p] = zmake<Z>(0, 0);
+    if (P.Fh) {
+      const int64_t NK = P.N * K;
+      const Z *c = P.Fh + base;
+      if (P.pair) {
+        const int H = P.Nw / 2;
+#pragma unroll
+        for (int r = 0; r < 5; ++r) {
+          Z v[KP];
+          ldg_chunk<Z, KP>(c + r * K, v);
+#pragma unroll
+          for (int p = 0; p < KP; ++p) {
+            zmac(f2[r][p], v[p], e2[0]);
+            zmac(f3[r][p], v[p], e3[0]);
+          }
+        }
+#pragma unroll 2
+        for (int s = 1; s <= 2 * H - 2; ++s) {
+          const auto w2 = pair_weight(e2, s, H), w3 = pair_weight(e3, s, H);
+#pragma unroll
+          for (int r = 0; r < 5; ++r) {
+            Z v[KP];
+            ldg_chunk<Z, KP>(c + (int64_t)s * NK + r * K, v);
+#pragma unroll
+            for (int p = 0; p < KP; ++p) {
+              f2[r][p].re = fma(w2, v[p].re, f2[r][p].re);
+              f2[r][p].im = fma(w2, v[p].im, f2[r][p].im);
+              f3[r][p].re = fma(w3, v[p].re, f3[r][p].re);
+              f3[r][p].im = fma(w3, v[p].im, f3[r][p].im);
+            }
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < 5; ++r) {
+          Z v[KP];
+          ldg_chunk<Z, KP>(c + (int64_t)(P.Nw - 1) * NK + r * K, v);
+#pragma unroll
+          for (int p = 0; p < KP; ++p) {
+            zmac(f2[r][p], v[p], e2[H]);
+            zmac(f3[r][p], v[p], e3[H]);
+          }
+        }
+      } else {
+#pragma unroll 2
+        for (int s = 0; s < P.Nw; ++s) {
+#pragma unroll
+          for (int r = 0; r < 5; ++r) {
+            Z v[KP];
+            ldg_chunk<Z, KP>(c + (int64_t)s * NK + r * K, v);
+#pragma unroll
+            for (int p = 0; p < KP; ++p) {
+              zmac(f2[r][p], v[p], e2[s]);
+              zmac(f3[r][p], v[p], e3[s]);
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      st_chunk<Z, KP>(P.F2 + base + r * K, f2[r]);
+      st_chunk<Z, KP>(P.F3 + base + r * K, f3[r]);
+    }
+  } else if (S == 2 || S == 3) {
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      Z yv[KP], t[KP], av[KP];
+      ldg_chunk<Z, KP>(P.y + base + r * K, yv);
+#pragma unroll
+      for (int p = 0; p < KP; ++p) t[p] = zaxpy(S == 2 ? P.dt_2 : P.dt, k[r][p], yv[p]);
+      st_chunk<Z, KP>((S == 2 ? P.zB : P.zA) + base + r * K, t);
+      ld_chunk<Z, KP>(P.acc + base + r * K, av);
+#pragma unroll
+      for (int p = 0; p < KP; ++p) av[p] = zaxpy(P.dt_62, k[r][p], av[p]);
+      st_chunk<Z, KP>(P.acc + base + r * K, av);
+    }
+  } else {
+    const int64_t ps = P.ring ? ring_slot(P.dir, i, P.Nt, P.R, P.Nstore) : -1;
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      Z av[KP];
+      ld_chunk<Z, KP>(P.acc + base + r * K, av);
+#pragma unroll
+      for (int p = 0; p < KP; ++p) av[p] = zaxpy(P.dt_6, k[r][p], av[p]);
+      st_chunk<Z, KP>(P.y + base + r * K, av);
+      if (ps >= 0) st_chunk<Z, KP>(P.ring + ps * P.N * K + base + r * K, av);
+    }
+    if (br == 0 && q == 0) P.step[0] = i + 1;
+  }
+}
+
 // Row of K complex values; 16-byte loads/stores (K even for complex64).
 template <class Z, int K>
 __device__ __forceinline__ void ld_row(const Z *p, Z (&v)[K]) {
@@ -290,10 +504,11 @@ __device__ __forceinline__ void forcing_row(const StepArgs<Z> &P, int64_t n, con
   }
 }
 
-static const int kRowThreads = 128;
-
+// One thread per row with all K test vectors in registers (complex128):
+// full warps, which is what matters when the FP64 pipe is the limit; the
+// lane-group kernel above leaves lanes idle for complex128 row groups.
 template <class Z, int K, int S>
-__global__ void __launch_bounds__(kRowThreads) k_bstage(const StepArgs<Z> P) {
+__global__ void __launch_bounds__(kRowThreads) k_rstage(const StepArgs<Z> P) {
   extern __shared__ unsigned char smem_raw[];
   Z *e2 = reinterpret_cast<Z *>(smem_raw);  // phasor rows of this step (stage 1)
   Z *e3 = e2 + P.Nw;
@@ -478,13 +693,27 @@ static StepArgs<Z> make_args(rsvdt_ctx *ctx, int dir, bool forced) {
 
 template <class Z, int K>
 static void launch_bstage(int stage, const StepArgs<Z> &P, cudaStream_t st) {
-  const int g = grid_for(P.N, kRowThreads);
+  constexpr int KP = (sizeof(Z) == 8 && K % 2 == 0) ? 2 : 1;
+  constexpr int L = K / KP;
+  constexpr int BPW = 32 / L;
+  const int64_t warps = (P.N / 5 + BPW - 1) / BPW;
+  const int g = grid_for(warps * 32, kRowThreads);
   const size_t sm = sizeof(Z) * 2 * (P.Nw > 0 ? P.Nw : 1);
+  if constexpr (sizeof(Z) == 16) {
+    const int gr = grid_for(P.N, kRowThreads);
+    switch (stage) {
+      case 1: k_rstage<Z, K, 1><<<gr, kRowThreads, sm, st>>>(P); break;
+      case 2: k_rstage<Z, K, 2><<<gr, kRowThreads, 0, st>>>(P); break;
+      case 3: k_rstage<Z, K, 3><<<gr, kRowThreads, 0, st>>>(P); break;
+      default: k_rstage<Z, K, 4><<<gr, kRowThreads, 0, st>>>(P); break;
+    }
+    return;
+  }
   switch (stage) {
-    case 1: k_bstage<Z, K, 1><<<g, kRowThreads, sm, st>>>(P); break;
-    case 2: k_bstage<Z, K, 2><<<g, kRowThreads, 0, st>>>(P); break;
-    case 3: k_bstage<Z, K, 3><<<g, kRowThreads, 0, st>>>(P); break;
-    default: k_bstage<Z, K, 4><<<g, kRowThreads, 0, st>>>(P); break;
+    case 1: k_bstage<Z, K, KP, 1><<<g, kRowThreads, sm, st>>>(P); break;
+    case 2: k_bstage<Z, K, KP, 2><<<g, kRowThreads, 0, st>>>(P); break;
+    case 3: k_bstage<Z, K, KP, 3><<<g, kRowThreads, 0, st>>>(P); break;
+    default: k_bstage<Z, K, KP, 4><<<g, kRowThreads, 0, st>>>(P); break;
   }
 }
 
