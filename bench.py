@@ -199,6 +199,72 @@ def time_to_gains(n: int, seed: int = 4321):
     return out
 
 
+def batch_form(count: int = 48, q: int = 0, seed: int = 2024):
+    """Batching form: `count` Ginzburg-Landau problems (N log-uniform in
+    [200, 20000], mu0 in [0.2, 0.45], k in {6, 10, 16}, Nw in {16, 32, 64};
+    grid spacing of the 500-node case, dt = T/4096, one transient period,
+    q = 0, discounting where a problem is unstable) solved one context after
+    another in complex128 (the plain method, 48 sequential solves) and as
+    one batch in complex128 and complex64. Wall time from the first action
+    to every problem's gains on the host; each batch is run once untimed
+    first (autotuning, graph capture), then re-run on the same sketches."""
+    import rsvdt
+    from rsvdt import synth
+
+    fam = synth.gl_family(count, seed=seed)
+    T = 2 * np.pi / 0.1
+    dt = T / 4096 * (1 + 1e-12)
+
+    def params(pr, prec):
+        return rsvdt.default_params(k=pr["k"], q=q, Nw=pr["Nw"], w=0.1, dt=dt, TransientLength=T,
+                                    DiscFlg=int(pr["beta"] > 0), beta=pr["beta"], precision=prec, Display=0)
+
+    sketches = [synth.complex_normal(pr["N"], pr["k"] * pr["Nw"], seed + 1 + i) for i, pr in enumerate(fam)]
+    S_seq = []
+    t0 = time.perf_counter()
+    for pr, F in zip(fam, sketches):
+        ctx = rsvdt.Context(params(pr, rsvdt.PREC_C128))
+        ctx.set_operator(pr["A"])
+        ctx.set_sketch(F)
+        ctx.run()
+        S_seq.append(ctx.get_results()[2])
+        ctx.close()
+    t_seq = time.perf_counter() - t0
+    out = {"workload": f"{count} Ginzburg-Landau problems, N {min(p['N'] for p in fam)}..{max(p['N'] for p in fam)} "
+                       f"(log-uniform), k in {{6,10,16}}, Nw in {{16,32,64}}, dt = T/4096, q = {q}, seed {seed}",
+           "sum_N_k": int(sum(p["N"] * p["k"] for p in fam)), "sequential_plain_c128_s": round(t_seq, 3)}
+    for name, prec in (("batched_c128", rsvdt.PREC_C128), ("batched_c64", rsvdt.PREC_C64)):
+        b = rsvdt.Batch(prec)
+        for pr in fam:
+            b.add(params(pr, prec), pr["A"])
+        for i, F in enumerate(sketches):
+            b.set_sketch(i, F)
+        b.run()
+        for i, F in enumerate(sketches):
+            b.set_sketch(i, F)
+        t0 = time.perf_counter()
+        b.run()
+        S_b = [b.get_results(i)[2] for i in range(len(fam))]
+        t_b = time.perf_counter() - t0
+        errs = [float((np.abs(Sb[:3] - Ss[:3]) / Ss[:3]).max()) for Sb, Ss in zip(S_b, S_seq)]
+        err1 = [float((np.abs(Sb[0] - Ss[0]) / Ss[0]).max()) for Sb, Ss in zip(S_b, S_seq)]
+        worst = int(np.argmax(errs))
+        err = errs[worst]
+        th, lanes, ms = b.tuning()
+        out[name + "_s"] = round(t_b, 3)
+        out[name + "_speedup_vs_sequential"] = round(t_seq / t_b, 3)
+        out[name + "_gain_rel_err_max_j<=3"] = err
+        out[name + "_gain1_rel_err_max"] = max(err1)
+        out[name + "_worst_problem"] = {"N": fam[worst]["N"], "mu0": round(fam[worst]["mu0"], 4),
+                                        "k": fam[worst]["k"], "Nw": fam[worst]["Nw"],
+                                        "beta": round(fam[worst]["beta"], 4),
+                                        "sigma1_max": float(S_seq[worst][0].max()),
+                                        "problems_over_1e-3": int(sum(e > 1e-3 for e in errs))}
+        out[name + "_tuned"] = {"threads": th, "lanes_per_row": lanes, "ms_per_batched_step": round(ms, 4)}
+        b.close()
+    return out
+
+
 def run_reference(args):
     """CPU arm: the reference algorithm on the host cores (oracle port)."""
     rank = int(os.environ.get("RANK", "0"))
@@ -236,6 +302,7 @@ def main():
     ap.add_argument("--n", type=int, default=64, help="3D grid size (64 for the benchmark)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-ttg", action="store_true", help="skip the time-to-gains solves")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batching-form comparison")
     ap.add_argument("--ttg-n", type=int, default=32, help="grid of the time-to-gains solves")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
@@ -334,6 +401,9 @@ def main():
     ttg = None
     if rank == 0 and not args.no_ttg:
         ttg = time_to_gains(args.ttg_n)
+    batching = None
+    if rank == 0 and not args.no_batch:
+        batching = batch_form()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -376,6 +446,7 @@ def main():
                     "api": "rsvdt_rk4_steps (host y, F3 in pinned memory)"},
             "cpu_baseline": cpu,
             "time_to_gains": ttg,
+            "batching": batching,
         }
         print(json.dumps(out))
     if dist:

@@ -193,6 +193,36 @@ rsvdt_status rsvdt_rk4_advance(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_
 rsvdt_status rsvdt_rk4_profile(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps,
                                double *stage_ms);
 
+/* ---------------------------------------------------------------- batching
+ * Many independent problems of uneven size (own operator, k, Nw, time
+ * grid, q) solved together: every action of the sequence runs for all
+ * problems at once, their RK4 steps advancing in lockstep with one launch
+ * per RK4 stage covering every problem's rows, replayed from a CUDA graph.
+ * The launch shape (threads per block, lanes per row) is chosen at the
+ * first run by timing candidates on the batch itself. The batch form of
+ * running SourceCode/main.c:134-144 for each problem in turn. */
+typedef struct rsvdt_batch rsvdt_batch;
+
+rsvdt_status rsvdt_batch_create(int32_t precision, rsvdt_batch **out);
+void rsvdt_batch_destroy(rsvdt_batch *b);
+const char *rsvdt_batch_last_error(const rsvdt_batch *b);
+/* Adds a problem with CSR operator A (as rsvdt_set_operator); the batch's
+ * precision overrides p->precision. *index receives its position. */
+rsvdt_status rsvdt_batch_add(rsvdt_batch *b, const rsvdt_params *p, int64_t N, const int64_t *rowptr,
+                             const int64_t *col, const double *val, int32_t *index);
+rsvdt_status rsvdt_batch_set_sketch(rsvdt_batch *b, int32_t index, const double *F, int64_t ld,
+                                    int64_t ncols);
+rsvdt_status rsvdt_batch_random_sketch(rsvdt_batch *b, int32_t index, uint64_t seed);
+/* Runs the whole sequence for every problem (q per problem). */
+rsvdt_status rsvdt_batch_run(rsvdt_batch *b);
+rsvdt_status rsvdt_batch_get_results(rsvdt_batch *b, int32_t index, double *U, int64_t ldu, double *V,
+                                     int64_t ldv, double *S);
+rsvdt_status rsvdt_batch_get_grid(const rsvdt_batch *b, int32_t index, rsvdt_grid *g);
+/* Launch shape chosen by the autotuner and its time per batched step. */
+rsvdt_status rsvdt_batch_get_tuning(const rsvdt_batch *b, int32_t *threads, int32_t *lanes_per_row,
+                                    double *ms_per_step);
+int64_t rsvdt_batch_launch_count(const rsvdt_batch *b);
+
 /* QR of every frequency block without allocating device memory.
  * No counterpart in the reference: it exists for callers that cannot call
  * cudaMalloc (work issued while another stream is being captured into a

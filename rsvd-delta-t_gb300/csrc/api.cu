@@ -411,7 +411,7 @@ void rsvdt_destroy(rsvdt_ctx *ctx) {
   free_graphs(ctx);
   for (void *p : ctx->allocations)
     if (p) cudaFree(p);
-  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->stream && ctx->owns_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
 
@@ -647,6 +647,19 @@ rsvdt_status rsvdt_get_block(rsvdt_ctx *ctx, double *Y, int64_t ld, int64_t *row
 rsvdt_status rsvdt_action(rsvdt_ctx *ctx, rsvdt_dir dir) {
   RSVDT_TRY(require_ready(ctx, true));
   const int d = dir == RSVDT_DIRECT ? 1 : 0;
+  int64_t rend = 0;
+  RSVDT_TRY(rsvdt::action_prepare(ctx, d, &rend));
+  RSVDT_TRY(run_steps(ctx, d, ctx->par.precision, 1, rend, true));
+  return rsvdt::action_finish(ctx, d);
+}
+
+}  // extern "C"
+
+namespace rsvdt {
+
+// First half of an action: weights before, forcing slabs, y = 0 and the
+// initial forcing; returns the number of RK4 steps (SourceCode/TSActionRK4.c:41-42).
+rsvdt_status action_prepare(rsvdt_ctx *ctx, int d, int64_t *rend_out) {
   const int prec = ctx->par.precision;
   RSVDT_TRY(check_weights(ctx));
   const int64_t rows_in = d ? ctx->Nb : ctx->Nc;
@@ -670,7 +683,14 @@ rsvdt_status rsvdt_action(rsvdt_ctx *ctx, rsvdt_dir dir) {
   RSVDT_TRY(stage_forcing(ctx, prec));
   if (!cuda_ok(ctx, cudaMemsetAsync(ctx->d_flags, 0, sizeof(int32_t) * 4, ctx->stream), "memset")) return RSVDT_ERR_CUDA;
   RSVDT_TRY(launch_forcing_init(ctx, d, prec));
-  RSVDT_TRY(run_steps(ctx, d, prec, 1, rend, true));
+  *rend_out = rend;
+  return RSVDT_OK;
+}
+
+// Second half: DFT or transient removal, weights after, finiteness check.
+rsvdt_status action_finish(rsvdt_ctx *ctx, int d) {
+  const int prec = ctx->par.precision;
+  const bool tr = ctx->par.TransientRemoval != 0;
   if (tr) {
     RSVDT_TRY(transient_removal(ctx, d, prec, ctx->blk2));
   } else {
@@ -692,6 +712,10 @@ rsvdt_status rsvdt_action(rsvdt_ctx *ctx, rsvdt_dir dir) {
   if (ctx->par.Display >= 1) printf("*** %s action done ***\n", d ? "Direct" : "Adjoint");
   return RSVDT_OK;
 }
+
+}  // namespace rsvdt
+
+extern "C" {
 
 rsvdt_status rsvdt_qr_all_freqs(rsvdt_ctx *ctx) {
   RSVDT_TRY(require_ready(ctx, true));

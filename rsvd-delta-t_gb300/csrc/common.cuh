@@ -123,6 +123,7 @@ struct rsvdt_ctx {
 
   int device = 0;
   cudaStream_t stream = nullptr;
+  bool owns_stream = true;  // false when the stream belongs to a batch
   int64_t launches = 0;
   std::string err;
 
@@ -182,6 +183,9 @@ inline int grid_for(int64_t n, int threads) {
 }
 
 // ------------------------------------------------- kernels (launchers)
+// api.cu (the two halves of an action around the RK4 steps)
+rsvdt_status action_prepare(rsvdt_ctx *ctx, int dir, int64_t *rend);
+rsvdt_status action_finish(rsvdt_ctx *ctx, int dir);
 // step.cu
 rsvdt_status stage_forcing_coeffs(rsvdt_ctx *ctx, int prec);
 rsvdt_status launch_forcing_init(rsvdt_ctx *ctx, int dir, int prec);
@@ -190,6 +194,13 @@ rsvdt_status run_steps(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_t ns
 rsvdt_status profile_steps(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_t nsteps,
                            double *stage_ms);
 rsvdt_status launch_dft(rsvdt_ctx *ctx, int prec, z128 *out);
+// Batched stepping of many contexts (step.cu); the argument blocks are
+// step_args_size(prec) bytes each.
+size_t step_args_size(int prec);
+void fill_step_args(rsvdt_ctx *ctx, int dir, int prec, int64_t rend, int64_t *shared_step, void *out);
+bool launch_batched_step(cudaStream_t st, int prec, const void *args, const int2 *work, int nwork, int threads,
+                         int fs, int64_t *step);
+void launch_set_step(cudaStream_t st, int64_t *step, int64_t i);
 rsvdt_status launch_unforced_steps(rsvdt_ctx *ctx, int dir, z128 *cols, int64_t ncols,
                                    int64_t nsteps);
 // dense.cu

@@ -37,6 +37,7 @@
 // (complex128: one thread per row with all k test vectors in registers,
 // full warps for the FP64-bound stages).
 #include <cstdarg>
+#include <cstring>
 
 #include "common.cuh"
 
@@ -57,6 +58,7 @@ struct StepArgs {
   Z *y, *zA, *zB, *acc, *F2, *F3, *ring;
   typename real_of<Z>::type dt, dt_2, dt_6, dt_62;  // dt, dt/2, dt/6, dt/6*2
   int64_t *step;
+  int64_t rend;  // last step of this problem's action (batched stepping)
 };
 
 // Half-step forcing indices of step i (SourceCode/TSRK4.c:21-26). For the
@@ -113,6 +115,61 @@ __device__ __forceinline__ Z forcing_at(const StepArgs<Z> &P, int64_t n, int kc,
   return f;
 }
 
+// Forcing at both times of a step (phasor rows e2, e3) for one (row, test
+// vector), in one pass over the slabs: lane fsub of an FS-lane group takes
+// slabs fsub, fsub + FS, ... (FS = 1: all of them); the pair slabs run in
+// two branch-free loops (weights Re e_f, then Im e_f), the two complex
+// slabs are added by the lanes that own them.
+template <class Z>
+__device__ __forceinline__ void forcing2(const StepArgs<Z> &P, int64_t n, int kc, const Z *e2, const Z *e3,
+                                         int fsub, int FS, Z &f2, Z &f3) {
+  const int64_t NK = P.N * P.K;
+  const Z *c = P.Fh + n * P.K + kc;
+  f2 = zmake<Z>(0, 0);
+  f3 = zmake<Z>(0, 0);
+  if (!P.pair) {
+#pragma unroll 4
+    for (int s = fsub; s < P.Nw; s += FS) {
+      const Z v = c[(int64_t)s * NK];
+      zmac(f2, v, e2[s]);
+      zmac(f3, v, e3[s]);
+    }
+    return;
+  }
+  const int H = P.Nw / 2, last = P.Nw - 1;
+  if (fsub == 0) {
+    const Z v = c[0];
+    zmac(f2, v, e2[0]);
+    zmac(f3, v, e3[0]);
+  }
+  // Slabs 1..H-1: c_f + c_{-f}, weight Re e_f (f = s).
+  int s = fsub == 0 ? FS : fsub;
+#pragma unroll 4
+  for (; s < H; s += FS) {
+    const Z v = c[(int64_t)s * NK];
+    const auto w2 = e2[s].re, w3 = e3[s].re;
+    f2.re = fma(w2, v.re, f2.re);
+    f2.im = fma(w2, v.im, f2.im);
+    f3.re = fma(w3, v.re, f3.re);
+    f3.im = fma(w3, v.im, f3.im);
+  }
+  // Slabs H..2H-2: i (c_f - c_{-f}), weight Im e_f (f = s - H + 1).
+#pragma unroll 4
+  for (; s < last; s += FS) {
+    const Z v = c[(int64_t)s * NK];
+    const auto w2 = e2[s - H + 1].im, w3 = e3[s - H + 1].im;
+    f2.re = fma(w2, v.re, f2.re);
+    f2.im = fma(w2, v.im, f2.im);
+    f3.re = fma(w3, v.re, f3.re);
+    f3.im = fma(w3, v.im, f3.im);
+  }
+  if (s == last) {
+    const Z v = c[(int64_t)last * NK];
+    zmac(f2, v, e2[H]);
+    zmac(f3, v, e3[H]);
+  }
+}
+
 // Sparse row product: acc += sum_j A[n,j] * x[j][kc].
 template <class Z>
 __device__ __forceinline__ void row_product(const StepArgs<Z> &P, int64_t n, int kc, const Z *x,
@@ -165,8 +222,7 @@ __global__ void __launch_bounds__(256) k_stage(const StepArgs<Z> P) {
     if (P.Fh) {
       int64_t j2, j3;
       step_idx(P.dir, i, P.two_ns, j2, j3);
-      f2 = forcing_at(P, n, kc, P.tab + j2 * P.Nw);
-      f3 = forcing_at(P, n, kc, P.tab + j3 * P.Nw);
+      forcing2(P, n, kc, P.tab + j2 * P.Nw, P.tab + j3 * P.Nw, 0, 1, f2, f3);
     }
     P.F2[t] = f2;
     P.F3[t] = f3;
@@ -686,6 +742,7 @@ static StepArgs<Z> make_args(rsvdt_ctx *ctx, int dir, bool forced) {
   P.dt_6 = (Rl)(dt / 6);
   P.dt_62 = (Rl)(dt / 6 * 2);
   P.step = ctx->d_step;
+  P.rend = INT64_MAX;
   return P;
 }
 
@@ -928,5 +985,158 @@ rsvdt_status launch_unforced_steps(rsvdt_ctx *ctx, int dir, z128 *cols, int64_t 
   if (!cuda_ok(ctx, cudaGetLastError(), "unforced steps")) return RSVDT_ERR_CUDA;
   return RSVDT_OK;
 }
+
+}  // namespace rsvdt
+
+// ------------------------------------------------------ batched stepping
+//
+// Many independent problems (own operator, k, Nw, time grid) advance in
+// lockstep: one launch per RK4 stage covers the rows of every problem. A
+// block works on one tile of one problem (work list entry (problem,
+// tile)); a problem past the last step of its action (step > rend) skips.
+// FS consecutive lanes share one (row, test vector): they split the
+// nonzeros (and, in stage 1, the forcing slabs) and combine their partial
+// sums with warp shuffles, which puts small problems on more lanes. The
+// launch shape (threads per block, FS) is chosen by the batch's autotuner.
+
+namespace rsvdt {
+
+template <class Z>
+__device__ __forceinline__ void row_product_split(const StepArgs<Z> &P, int64_t n, int kc, const Z *x, Z &acc,
+                                                  int fsub, int FS) {
+  const int K = P.K;
+  if (P.bs == 0) {
+    const int32_t b = __ldg(P.rowptr + n), e = __ldg(P.rowptr + n + 1);
+    for (int32_t j = b + fsub; j < e; j += FS) zmac(acc, P.val[j], x[(int64_t)__ldg(P.col + j) * K + kc]);
+  } else {
+    const int bs = P.bs;
+    const int64_t br = n / bs;
+    const int r = (int)(n - br * bs);
+    const int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
+    for (int32_t j = b + fsub; j < e; j += FS) {
+      const int64_t c0 = (int64_t)__ldg(P.col + j) * bs;
+      const Z *blkrow = P.val + ((int64_t)j * bs + r) * bs;
+      for (int c = 0; c < bs; ++c) zmac(acc, blkrow[c], x[(c0 + c) * K + kc]);
+    }
+  }
+}
+
+template <class Z, int FS>
+__device__ __forceinline__ void group_sum(Z &v) {
+#pragma unroll
+  for (int off = FS / 2; off > 0; off >>= 1) {
+    v.re += __shfl_xor_sync(0xffffffffu, v.re, off);
+    v.im += __shfl_xor_sync(0xffffffffu, v.im, off);
+  }
+}
+
+template <class Z, int S, int FS>
+__global__ void __launch_bounds__(256) k_stage_batched(const StepArgs<Z> *__restrict__ probs,
+                                                       const int2 *__restrict__ work, int64_t *step) {
+  const int2 wk = work[blockIdx.x];
+  const StepArgs<Z> &P = probs[wk.x];
+  const int64_t i = (S == 1) ? step[0] : step[1];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (S == 1) step[1] = i;
+    if (S == 4) step[0] = i + 1;
+  }
+  if (i > P.rend) return;  // uniform over the block (one problem per block)
+  const int64_t local = (int64_t)wk.y * blockDim.x + threadIdx.x;
+  const int64_t u = local / FS;
+  const int fsub = (int)(local - u * FS);
+  const int64_t NK = P.N * P.K;
+  const bool valid = u < NK;
+  const int64_t n = valid ? u / P.K : 0;
+  const int kc = valid ? (int)(u - n * P.K) : 0;
+  const Z *x = (S == 1) ? P.y : (S == 2) ? P.zA : (S == 3) ? P.zB : P.zA;
+  Z k = zmake<Z>(0, 0), f2 = zmake<Z>(0, 0), f3 = zmake<Z>(0, 0);
+  if (valid) {
+    row_product_split(P, n, kc, x, k, fsub, FS);
+    if (S == 1 && P.Fh) {
+      int64_t j2, j3;
+      step_idx(P.dir, i, P.two_ns, j2, j3);
+      forcing2(P, n, kc, P.tab + j2 * P.Nw, P.tab + j3 * P.Nw, fsub, FS, f2, f3);
+    }
+  }
+  if (FS > 1) {
+    group_sum<Z, FS>(k);
+    if (S == 1) {
+      group_sum<Z, FS>(f2);
+      group_sum<Z, FS>(f3);
+    }
+  }
+  if (!valid || fsub != 0) return;
+  const int64_t t = u;
+  const Z addv = (S == 1 || S == 4) ? P.F3[t] : P.F2[t];
+  k.re += addv.re;
+  k.im += addv.im;
+  const Z yv = P.y[t];
+  if (S == 1) {
+    P.F2[t] = f2;
+    P.F3[t] = f3;
+    P.zA[t] = zaxpy(P.dt_2, k, yv);
+    P.acc[t] = zaxpy(P.dt_6, k, yv);
+  } else if (S == 2) {
+    P.zB[t] = zaxpy(P.dt_2, k, yv);
+    P.acc[t] = zaxpy(P.dt_62, k, P.acc[t]);
+  } else if (S == 3) {
+    P.zA[t] = zaxpy(P.dt, k, yv);
+    P.acc[t] = zaxpy(P.dt_62, k, P.acc[t]);
+  } else {
+    const Z ynew = zaxpy(P.dt_6, k, P.acc[t]);
+    P.y[t] = ynew;
+    const int64_t p = P.ring ? ring_slot(P.dir, i, P.Nt, P.R, P.Nstore) : -1;
+    if (p >= 0) P.ring[p * NK + t] = ynew;
+  }
+}
+
+size_t step_args_size(int prec) { return prec == RSVDT_PREC_C64 ? sizeof(StepArgs<z64>) : sizeof(StepArgs<z128>); }
+
+// Host copy of ctx's stage arguments for direction dir with the batch's
+// shared step counter and the action's last step.
+void fill_step_args(rsvdt_ctx *ctx, int dir, int prec, int64_t rend, int64_t *shared_step, void *out) {
+  if (prec == RSVDT_PREC_C64) {
+    auto P = make_args<z64>(ctx, dir, true);
+    P.step = shared_step;
+    P.rend = rend;
+    memcpy(out, &P, sizeof P);
+  } else {
+    auto P = make_args<z128>(ctx, dir, true);
+    P.step = shared_step;
+    P.rend = rend;
+    memcpy(out, &P, sizeof P);
+  }
+}
+
+template <class Z, int FS>
+static void launch_batched_fs(cudaStream_t st, const void *args, const int2 *work, int nwork, int threads,
+                              int64_t *step) {
+  const StepArgs<Z> *P = (const StepArgs<Z> *)args;
+  k_stage_batched<Z, 1, FS><<<nwork, threads, 0, st>>>(P, work, step);
+  k_stage_batched<Z, 2, FS><<<nwork, threads, 0, st>>>(P, work, step);
+  k_stage_batched<Z, 3, FS><<<nwork, threads, 0, st>>>(P, work, step);
+  k_stage_batched<Z, 4, FS><<<nwork, threads, 0, st>>>(P, work, step);
+}
+
+template <class Z>
+static bool launch_batched_t(cudaStream_t st, const void *args, const int2 *work, int nwork, int threads, int fs,
+                             int64_t *step) {
+  switch (fs) {
+    case 1: launch_batched_fs<Z, 1>(st, args, work, nwork, threads, step); return true;
+    case 2: launch_batched_fs<Z, 2>(st, args, work, nwork, threads, step); return true;
+    case 4: launch_batched_fs<Z, 4>(st, args, work, nwork, threads, step); return true;
+    case 8: launch_batched_fs<Z, 8>(st, args, work, nwork, threads, step); return true;
+    default: return false;
+  }
+}
+
+// One batched RK4 step (four launches) on stream st.
+bool launch_batched_step(cudaStream_t st, int prec, const void *args, const int2 *work, int nwork, int threads,
+                         int fs, int64_t *step) {
+  if (prec == RSVDT_PREC_C64) return launch_batched_t<z64>(st, args, work, nwork, threads, fs, step);
+  return launch_batched_t<z128>(st, args, work, nwork, threads, fs, step);
+}
+
+void launch_set_step(cudaStream_t st, int64_t *step, int64_t i) { k_set_step<<<1, 1, 0, st>>>(step, i); }
 
 }  // namespace rsvdt

@@ -39,6 +39,9 @@ EXPORTED = [
     "rsvdt_get_results", "rsvdt_rk4_steps", "rsvdt_rk4_reset", "rsvdt_rk4_advance",
     "rsvdt_rk4_profile", "rsvdt_synchronize", "rsvdt_stream", "rsvdt_launch_count",
     "rsvdt_qr_all_freqs_noalloc",
+    "rsvdt_batch_create", "rsvdt_batch_destroy", "rsvdt_batch_last_error", "rsvdt_batch_add",
+    "rsvdt_batch_set_sketch", "rsvdt_batch_random_sketch", "rsvdt_batch_run", "rsvdt_batch_get_results",
+    "rsvdt_batch_get_grid", "rsvdt_batch_get_tuning", "rsvdt_batch_launch_count",
 ]
 
 
@@ -117,6 +120,17 @@ def load_library(path: str | None = None) -> C.CDLL:
         "rsvdt_rk4_advance": (C.c_int, [vp, C.c_int, i64, i64]),
         "rsvdt_rk4_profile": (C.c_int, [vp, C.c_int, i64, i64, d]),
         "rsvdt_qr_all_freqs_noalloc": (C.c_int, [vp, vp, i64, i64, i64, vp, C.c_char_p, i64]),
+        "rsvdt_batch_create": (C.c_int, [C.c_int32, P(vp)]),
+        "rsvdt_batch_destroy": (None, [vp]),
+        "rsvdt_batch_last_error": (C.c_char_p, [vp]),
+        "rsvdt_batch_add": (C.c_int, [vp, P(Params), i64, P(i64), P(i64), d, P(C.c_int32)]),
+        "rsvdt_batch_set_sketch": (C.c_int, [vp, C.c_int32, d, i64, i64]),
+        "rsvdt_batch_random_sketch": (C.c_int, [vp, C.c_int32, C.c_uint64]),
+        "rsvdt_batch_run": (C.c_int, [vp]),
+        "rsvdt_batch_get_results": (C.c_int, [vp, C.c_int32, d, i64, d, i64, d]),
+        "rsvdt_batch_get_grid": (C.c_int, [vp, C.c_int32, P(Grid)]),
+        "rsvdt_batch_get_tuning": (C.c_int, [vp, P(C.c_int32), P(C.c_int32), d]),
+        "rsvdt_batch_launch_count": (i64, [vp]),
         "rsvdt_synchronize": (C.c_int, [vp]),
         "rsvdt_stream": (vp, [vp]),
         "rsvdt_launch_count": (i64, [vp]),
@@ -307,3 +321,80 @@ class Context:
 
     def launch_count(self) -> int:
         return int(self._lib.rsvdt_launch_count(self._h))
+
+
+class Batch:
+    """Many independent problems solved together (rsvdt_batch_*): every
+    action runs for all problems at once with lockstep batched RK4 stages."""
+
+    def __init__(self, precision: int = PREC_C128):
+        self._lib = load_library()
+        self._h = C.c_void_p()
+        self._k = []
+        st = self._lib.rsvdt_batch_create(precision, C.byref(self._h))
+        if st != OK:
+            msg = self._lib.rsvdt_batch_last_error(self._h).decode() if self._h else "batch creation failed"
+            self.close()
+            raise RsvdtError(st, msg)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.rsvdt_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int):
+        if st != OK:
+            raise RsvdtError(st, self._lib.rsvdt_batch_last_error(self._h).decode())
+
+    def add(self, params: Params, A) -> int:
+        A = A.tocsr()
+        A.sort_indices()
+        rp, ci, va = _csr_arrays(A.indptr, A.indices, A.data)
+        idx = C.c_int32()
+        self._check(self._lib.rsvdt_batch_add(self._h, C.byref(params), A.shape[0], _iptr(rp), _iptr(ci),
+                                              _dptr(va.view(np.float64)), C.byref(idx)))
+        self._k.append(int(params.k))
+        return idx.value
+
+    def grid(self, index: int) -> Grid:
+        g = Grid()
+        self._check(self._lib.rsvdt_batch_get_grid(self._h, index, C.byref(g)))
+        return g
+
+    def set_sketch(self, index: int, F: np.ndarray) -> None:
+        F = np.asfortranarray(F, dtype=np.complex128)
+        self._check(self._lib.rsvdt_batch_set_sketch(self._h, index, F.ctypes.data_as(C.POINTER(C.c_double)),
+                                                     F.shape[0], F.shape[1]))
+        self._k[index] = F.shape[1] // self.grid(index).Nw_eff
+
+    def random_sketch(self, index: int, seed: int) -> None:
+        self._check(self._lib.rsvdt_batch_random_sketch(self._h, index, seed))
+
+    def run(self) -> None:
+        self._check(self._lib.rsvdt_batch_run(self._h))
+
+    def get_results(self, index: int):
+        g = self.grid(index)
+        k = self._k[index]
+        ncol = k * g.Nw_eff
+        U = np.zeros((g.Nc, ncol), dtype=np.complex128, order="F")
+        V = np.zeros((g.Nb, ncol), dtype=np.complex128, order="F")
+        S = np.zeros((k, g.Nw_eff), dtype=np.float64, order="F")
+        self._check(self._lib.rsvdt_batch_get_results(self._h, index, U.ctypes.data_as(C.POINTER(C.c_double)), g.Nc,
+                                                      V.ctypes.data_as(C.POINTER(C.c_double)), g.Nb,
+                                                      S.ctypes.data_as(C.POINTER(C.c_double))))
+        return U, V, S
+
+    def tuning(self):
+        th, fs, ms = C.c_int32(), C.c_int32(), C.c_double()
+        self._check(self._lib.rsvdt_batch_get_tuning(self._h, C.byref(th), C.byref(fs), C.byref(ms)))
+        return th.value, fs.value, ms.value
+
+    def launch_count(self) -> int:
+        return int(self._lib.rsvdt_batch_launch_count(self._h))

@@ -27,6 +27,59 @@ def gl_operator(N: int = 500, L: float = 50.0, nu: complex = 2 + 0.2j, gamma: co
     return A
 
 
+def gl_stretched(N: int, mu0: float, nu: complex = 2 + 0.2j, gamma: complex = 1 - 1j,
+                 mu2: float = -0.005) -> sp.csr_matrix:
+    """Ginzburg-Landau operator on N nodes with the grid spacing of the
+    500-node case: domain [-L, L] with L = 50 (N+1)/501 and the mu profile
+    stretched with it, mu(x) = mu0 + mu2 (50 x / L)^2. The largest |lambda|
+    stays near 150 for every N, so one time step (T/4096 at w0 = 0.1) suits
+    the whole family."""
+    L = 50.0 * (N + 1) / 501
+    x = np.linspace(-L, L, N + 2)[1:-1]
+    h = x[1] - x[0]
+    lower = nu / (2 * h) + gamma / h**2
+    upper = -nu / (2 * h) + gamma / h**2
+    diag = -2 * gamma / h**2 + (mu0 + mu2 * (50 * x / L) ** 2)
+    A = sp.diags([np.full(N - 1, lower), diag.astype(complex), np.full(N - 1, upper)], [-1, 0, 1],
+                 shape=(N, N), format="csr", dtype=np.complex128)
+    A.sort_indices()
+    return A
+
+
+def gl_rightmost(N: int, mu0: float, nu: complex = 2 + 0.2j, gamma: complex = 1 - 1j,
+                 mu2: float = -0.005) -> float:
+    """Real part of the leading global eigenvalue of gl_stretched's
+    operator, lambda_0 = mu0 - nu^2/(4 gamma) - sqrt(-m gamma) with
+    m = mu2 (50/L)^2 the profile's curvature (the harmonic-oscillator
+    spectrum of the Ginzburg-Landau operator with a quadratic mu). Iterative
+    eigensolvers are unreliable here: the operator is strongly non-normal."""
+    L = 50.0 * (N + 1) / 501
+    m = mu2 * (50.0 / L) ** 2
+    lam0 = mu0 - nu**2 / (4 * gamma) - np.sqrt(-m * gamma + 0j)
+    return float(lam0.real)
+
+
+def gl_family(count: int = 48, seed: int = 2024, n_lo: int = 200, n_hi: int = 20000,
+              ks=(6, 10, 16), nws=(16, 32, 64), margin: float = 0.05):
+    """The batching family: `count` Ginzburg-Landau problems with N
+    log-uniform in [n_lo, n_hi], mu0 uniform in [0.2, 0.45], k and Nw drawn
+    from `ks` and `nws`. A problem whose rightmost eigenvalue is above
+    -margin gets the reference's discounting A <- A - beta I with beta
+    placing it at -margin (SourceCode/LNSStructure.c:53-56)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        N = int(round(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi)))))
+        mu0 = float(rng.uniform(0.2, 0.45))
+        k = int(rng.choice(ks))
+        nw = int(rng.choice(nws))
+        A = gl_stretched(N, mu0)
+        lr = gl_rightmost(N, mu0)
+        beta = max(0.0, lr + margin)
+        out.append(dict(N=N, mu0=mu0, k=k, Nw=nw, A=A, beta=beta, rightmost=lr))
+    return out
+
+
 def complex_normal(rows: int, cols: int, seed: int) -> np.ndarray:
     """i.i.d. CN(0,1) = (a + ib)/sqrt(2), a, b ~ N(0,1) from
     numpy.random.default_rng(seed); Fortran order."""

@@ -1,0 +1,95 @@
+"""Batching form: problems of uneven N, k, Nw and q solved together
+(rsvdt_batch_*) give the same results as solving each on its own context
+(the reference's main.c sequence, SourceCode/main.c:134-144, per problem)."""
+import numpy as np
+import pytest
+
+from rsvdt import synth
+
+pytestmark = pytest.mark.gpu
+
+W0 = 0.1
+
+
+def family():
+    # (N, mu0, k, Nw, q): uneven sizes, test-vector counts, frequencies, q.
+    specs = [(64, 0.2, 2, 8, 0), (150, 0.3, 3, 16, 1), (97, 0.25, 4, 8, 1), (233, 0.4, 2, 16, 0),
+             (400, 0.35, 3, 8, 0)]
+    T = 2 * np.pi / W0
+    dt = T / 4096 * (1 + 1e-12)
+    out = []
+    for i, (N, mu0, k, nw, q) in enumerate(specs):
+        A = synth.gl_stretched(N, mu0)
+        F = synth.complex_normal(N, k * nw, 100 + i)
+        out.append(dict(A=A, k=k, Nw=nw, q=q, F=F, dt=dt, T=T))
+    return out
+
+
+def params_of(rsvdt, pr, prec=0):
+    return rsvdt.default_params(k=pr["k"], q=pr["q"], Nw=pr["Nw"], w=W0, dt=pr["dt"], TransientLength=pr["T"],
+                                precision=prec, Display=0)
+
+
+def solve_alone(rsvdt, pr, prec=0):
+    ctx = rsvdt.Context(params_of(rsvdt, pr, prec))
+    ctx.set_operator(pr["A"])
+    ctx.set_sketch(pr["F"])
+    ctx.run()
+    out = ctx.get_results()
+    ctx.close()
+    return out
+
+
+def mode_angle(U, Uref, k, nw):
+    ang = 0.0
+    for iw in range(nw):
+        u = U[:, iw * k] / np.linalg.norm(U[:, iw * k])
+        v = Uref[:, iw * k] / np.linalg.norm(Uref[:, iw * k])
+        c = np.vdot(v, u)
+        ang = max(ang, 2 * np.arcsin(min(1.0, np.linalg.norm(u - c / abs(c) * v) / 2)))
+    return ang
+
+
+def test_batch_matches_one_context_per_problem(built_lib):
+    import rsvdt
+    fam = family()
+    b = rsvdt.Batch(rsvdt.PREC_C128)
+    for pr in fam:
+        i = b.add(params_of(rsvdt, pr), pr["A"])
+        b.set_sketch(i, pr["F"])
+    b.run()
+    threads, lanes, ms = b.tuning()
+    assert threads in (128, 256) and lanes in (1, 2, 4, 8) and ms > 0
+    for i, pr in enumerate(fam):
+        U, V, S = b.get_results(i)
+        Ur, Vr, Sr = solve_alone(rsvdt, pr)
+        # Batched stages sum nonzeros and forcing slabs over several lanes:
+        # same operations, different summation order.
+        assert (np.abs(S - Sr) / Sr).max() < 1e-9, i
+        assert mode_angle(U, Ur, pr["k"], pr["Nw"]) < 1e-7
+        assert mode_angle(V, Vr, pr["k"], pr["Nw"]) < 1e-7
+    b.close()
+
+
+def test_batch_precision_form_close_to_plain(built_lib):
+    import rsvdt
+    fam = family()
+    b = rsvdt.Batch(rsvdt.PREC_C64)
+    for pr in fam:
+        i = b.add(params_of(rsvdt, pr), pr["A"])
+        b.set_sketch(i, pr["F"])
+    b.run()
+    for i, pr in enumerate(fam):
+        _, _, S = b.get_results(i)
+        _, _, Sr = solve_alone(rsvdt, pr)
+        assert (np.abs(S[0] - Sr[0]) / Sr[0]).max() < 1e-3, i
+    b.close()
+
+
+def test_batch_errors(built_lib):
+    import rsvdt
+    b = rsvdt.Batch()
+    with pytest.raises(rsvdt.RsvdtError) as e:
+        b.run()
+    assert e.value.status == rsvdt.ERR_STATE
+    b.close()
