@@ -265,6 +265,49 @@ def batch_form(count: int = 48, q: int = 0, seed: int = 2024):
     return out
 
 
+def learned_form(n_train: int = 200, n_held: int = 50, N: int = 2000, seed: int = 77):
+    """Learned-sketch form on the Ginzburg-Landau family (N = 2000, k = 10,
+    Nw = 16; mu0 in [0.2, 0.45], U in [1.5, 2.5]): the method's own forcing
+    modes at n_train seeded points (complex64 batch, q = 1), r = 64 POD
+    basis, network 3 -> 4 x 256 GELU -> 2 r k trained on the GPU; at n_held
+    held-out points, q = 0 from the learned sketch against q = 0, 1, 2 from
+    random sketches, gains measured against a converged solve (complex128,
+    q = 3). Problems whose FP64 gain check exceeds 1e-3 are counted as
+    falling back to the random sketch with q = 1."""
+    import rsvdt
+    from rsvdt import learned
+
+    fam = learned.Family(N=N, k=10, Nw=16)
+    train = fam.points(n_train, seed=seed)
+    held = fam.points(n_held, seed=seed + 1)
+    res, t_data = learned.solve_batch(fam, train, q=1, precision=rsvdt.PREC_C64, seed=seed * 10)
+    ls = learned.LearnedSketch(fam, r=64, hidden=256, depth=4, seed=1)
+    t0 = time.perf_counter()
+    ls.fit(train, [V for (_, V, _) in res], steps=4000, batch=256, lr=1e-3)
+    t_fit = time.perf_counter() - t0
+    ref, t_ref = learned.solve_batch(fam, held, q=3, precision=rsvdt.PREC_C128, seed=seed * 20)
+    out = {"workload": f"Ginzburg-Landau family N={N}, k=10, Nw=16; {n_train} training / {n_held} held-out points",
+           "training_data_s": round(t_data, 3), "fit_s": round(t_fit, 3), "train_s_on_gpu": round(ls.train_seconds, 3),
+           "pod_energy_r64": round(ls.pod_energy, 6), "final_loss": ls.final_loss, "reference_q3_s": round(t_ref, 3)}
+    t0 = time.perf_counter()
+    sk = [ls.sketch(p) for p in held]
+    t_inf = time.perf_counter() - t0
+    runs = {"learned_q0": (0, sk)}
+    for q in (0, 1, 2):
+        runs[f"random_q{q}"] = (q, None)
+    for name, (q, s) in runs.items():
+        r, t = learned.solve_batch(fam, held, q=q, precision=rsvdt.PREC_C128, sketches=s, seed=seed * 30)
+        e1, e3 = learned.gain_errors(r, ref)
+        out[name] = {"solve_s": round(t, 3), "gain1_err_median": float(np.median(e1)), "gain1_err_max": float(e1.max()),
+                     "gain_j<=3_err_median": float(np.median(e3)), "within_1e-3": int((e3 <= 1e-3).sum())}
+        if name == "learned_q0":
+            checks = [learned.gain_check(fam, p, rr) for p, rr in zip(held, r)]
+            out[name]["inference_s"] = round(t_inf, 3)
+            out[name]["fallbacks"] = int(sum(c > 1e-3 for c in checks))
+            out[name]["gain_check_median"] = float(np.median(checks))
+    return out
+
+
 def run_reference(args):
     """CPU arm: the reference algorithm on the host cores (oracle port)."""
     rank = int(os.environ.get("RANK", "0"))
@@ -303,6 +346,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-ttg", action="store_true", help="skip the time-to-gains solves")
     ap.add_argument("--no-batch", action="store_true", help="skip the batching-form comparison")
+    ap.add_argument("--learned", action="store_true", help="run the learned-sketch experiment (about a minute)")
     ap.add_argument("--ttg-n", type=int, default=32, help="grid of the time-to-gains solves")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
@@ -404,6 +448,9 @@ def main():
     batching = None
     if rank == 0 and not args.no_batch:
         batching = batch_form()
+    learned_res = None
+    if rank == 0 and args.learned:
+        learned_res = learned_form()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -447,6 +494,7 @@ def main():
             "cpu_baseline": cpu,
             "time_to_gains": ttg,
             "batching": batching,
+            "learned_sketch": learned_res,
         }
         print(json.dumps(out))
     if dist:

@@ -223,6 +223,34 @@ rsvdt_status rsvdt_batch_get_tuning(const rsvdt_batch *b, int32_t *threads, int3
                                     double *ms_per_step);
 int64_t rsvdt_batch_launch_count(const rsvdt_batch *b);
 
+/* ------------------------------------------------------- learned sketch
+ * Multilayer perceptron (GELU between layers, linear output) that maps a
+ * problem's parameters to the coefficients of a warm-start test matrix in
+ * a POD basis. bf16 weights, FP32 activations, products and gradients;
+ * trained with Adam on a mean-squared-error loss. Inference and training
+ * kernels are the library's own. No counterpart in the reference, whose
+ * sketch is always random (SourceCode/CreateRandomMat.c:33-39). */
+typedef struct rsvdt_mlp rsvdt_mlp;
+
+/* widths: n_layers + 1 entries (input, hidden..., output). */
+rsvdt_status rsvdt_mlp_create(int32_t n_layers, const int32_t *widths, uint64_t seed, rsvdt_mlp **out);
+void rsvdt_mlp_destroy(rsvdt_mlp *n);
+const char *rsvdt_mlp_last_error(const rsvdt_mlp *n);
+/* Flat FP32 parameters: for each layer, W (out x in, row-major) then b. */
+int64_t rsvdt_mlp_param_count(const rsvdt_mlp *n);
+rsvdt_status rsvdt_mlp_set_params(rsvdt_mlp *n, const float *params);
+rsvdt_status rsvdt_mlp_get_params(rsvdt_mlp *n, float *params);
+/* Y (rows x out) = network(X (rows x in)); host arrays. */
+rsvdt_status rsvdt_mlp_forward(rsvdt_mlp *n, const float *X, int64_t rows, float *Y);
+/* Mean squared error against T and its gradient (flat, like the params). */
+rsvdt_status rsvdt_mlp_gradients(rsvdt_mlp *n, const float *X, const float *T, int64_t rows, float *loss,
+                                 float *grads);
+/* Adam (lr, beta1 0.9, beta2 0.999) for `steps` minibatches of `batch`
+ * rows drawn without replacement per epoch; the data set is copied to the
+ * device once. final_loss: loss of the last minibatch. */
+rsvdt_status rsvdt_mlp_train(rsvdt_mlp *n, const float *X, const float *T, int64_t samples, int64_t batch,
+                             int64_t steps, float lr, uint64_t seed, float *final_loss);
+
 /* QR of every frequency block without allocating device memory.
  * No counterpart in the reference: it exists for callers that cannot call
  * cudaMalloc (work issued while another stream is being captured into a

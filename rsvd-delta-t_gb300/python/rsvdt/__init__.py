@@ -42,6 +42,9 @@ EXPORTED = [
     "rsvdt_batch_create", "rsvdt_batch_destroy", "rsvdt_batch_last_error", "rsvdt_batch_add",
     "rsvdt_batch_set_sketch", "rsvdt_batch_random_sketch", "rsvdt_batch_run", "rsvdt_batch_get_results",
     "rsvdt_batch_get_grid", "rsvdt_batch_get_tuning", "rsvdt_batch_launch_count",
+    "rsvdt_mlp_create", "rsvdt_mlp_destroy", "rsvdt_mlp_last_error", "rsvdt_mlp_param_count",
+    "rsvdt_mlp_set_params", "rsvdt_mlp_get_params", "rsvdt_mlp_forward", "rsvdt_mlp_gradients",
+    "rsvdt_mlp_train",
 ]
 
 
@@ -131,6 +134,16 @@ def load_library(path: str | None = None) -> C.CDLL:
         "rsvdt_batch_get_grid": (C.c_int, [vp, C.c_int32, P(Grid)]),
         "rsvdt_batch_get_tuning": (C.c_int, [vp, P(C.c_int32), P(C.c_int32), d]),
         "rsvdt_batch_launch_count": (i64, [vp]),
+        "rsvdt_mlp_create": (C.c_int, [C.c_int32, P(C.c_int32), C.c_uint64, P(vp)]),
+        "rsvdt_mlp_destroy": (None, [vp]),
+        "rsvdt_mlp_last_error": (C.c_char_p, [vp]),
+        "rsvdt_mlp_param_count": (i64, [vp]),
+        "rsvdt_mlp_set_params": (C.c_int, [vp, P(C.c_float)]),
+        "rsvdt_mlp_get_params": (C.c_int, [vp, P(C.c_float)]),
+        "rsvdt_mlp_forward": (C.c_int, [vp, P(C.c_float), i64, P(C.c_float)]),
+        "rsvdt_mlp_gradients": (C.c_int, [vp, P(C.c_float), P(C.c_float), i64, P(C.c_float), P(C.c_float)]),
+        "rsvdt_mlp_train": (C.c_int, [vp, P(C.c_float), P(C.c_float), i64, i64, i64, C.c_float, C.c_uint64,
+                                      P(C.c_float)]),
         "rsvdt_synchronize": (C.c_int, [vp]),
         "rsvdt_stream": (vp, [vp]),
         "rsvdt_launch_count": (i64, [vp]),
@@ -398,3 +411,73 @@ class Batch:
 
     def launch_count(self) -> int:
         return int(self._lib.rsvdt_batch_launch_count(self._h))
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Mlp:
+    """The learned sketch's network (rsvdt_mlp_*): GELU MLP with bf16
+    weights and FP32 accumulation, trained on the GPU."""
+
+    def __init__(self, widths, seed: int = 0):
+        self._lib = load_library()
+        self._h = C.c_void_p()
+        self.widths = [int(x) for x in widths]
+        w = (C.c_int32 * len(self.widths))(*self.widths)
+        st = self._lib.rsvdt_mlp_create(len(self.widths) - 1, w, seed, C.byref(self._h))
+        if st != OK:
+            msg = self._lib.rsvdt_mlp_last_error(self._h).decode() if self._h else "network creation failed"
+            self.close()
+            raise RsvdtError(st, msg)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.rsvdt_mlp_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != OK:
+            raise RsvdtError(st, self._lib.rsvdt_mlp_last_error(self._h).decode())
+
+    @property
+    def n_params(self) -> int:
+        return int(self._lib.rsvdt_mlp_param_count(self._h))
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.n_params, dtype=np.float32)
+        self._check(self._lib.rsvdt_mlp_get_params(self._h, _fptr(p)))
+        return p
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._check(self._lib.rsvdt_mlp_set_params(self._h, _fptr(p)))
+
+    def forward(self, X: np.ndarray) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros((X.shape[0], self.widths[-1]), dtype=np.float32)
+        self._check(self._lib.rsvdt_mlp_forward(self._h, _fptr(X), X.shape[0], _fptr(Y)))
+        return Y
+
+    def gradients(self, X: np.ndarray, T: np.ndarray):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        g = np.zeros(self.n_params, dtype=np.float32)
+        loss = C.c_float()
+        self._check(self._lib.rsvdt_mlp_gradients(self._h, _fptr(X), _fptr(T), X.shape[0], C.byref(loss), _fptr(g)))
+        return float(loss.value), g
+
+    def train(self, X: np.ndarray, T: np.ndarray, batch: int, steps: int, lr: float, seed: int = 0) -> float:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        loss = C.c_float()
+        self._check(self._lib.rsvdt_mlp_train(self._h, _fptr(X), _fptr(T), X.shape[0], batch, steps, lr, seed,
+                                              C.byref(loss)))
+        return float(loss.value)

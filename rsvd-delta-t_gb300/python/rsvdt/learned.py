@@ -1,0 +1,185 @@
+"""Learned sketch: a network trained on the method's own forcing modes
+predicts the warm-start test matrix of a new problem, replacing the random
+sketch (SourceCode/CreateRandomMat.c:33-39) so that fewer power iterations
+are needed.
+
+Pipeline (everything heavy runs on the GPU through the C ABI):
+  1. the method itself (batched RSVD-Delta-t) computes the top-k forcing
+     modes V(p, w) at seeded training points p of a problem family;
+  2. a POD basis Phi (N x r) of all those modes;
+  3. each mode block projected on Phi, C = Phi^H V (r x k), column phases
+     fixed (largest coefficient real and positive), real and imaginary parts
+     standardised;
+  4. the network (3 -> hidden^depth GELU -> 2 r k; bf16 weights, FP32
+     accumulation; rsvdt_mlp_*) is trained with Adam on inputs
+     (p_1, p_2, w) scaled to [-1, 1];
+  5. for a new problem the sketch's frequency block iw is Phi C_pred(p, w_iw).
+The fallback is the random sketch: after a learned run, one FP64 direct
+action on the computed forcing modes checks the gains (| |R v_j| - s_j | /
+s_j for the leading modes); above the threshold the problem is re-solved
+from a random sketch with one power iteration.
+
+Problem family: Ginzburg-Landau operators with the grid spacing of the
+500-node case (synth.gl_stretched), parameters mu0 in [0.2, 0.45] and the
+advection speed U = Re(nu) in [1.5, 2.5], discounted where unstable.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import synth
+
+
+@dataclass
+class Family:
+    N: int = 2000
+    k: int = 10
+    Nw: int = 16
+    w0: float = 0.1
+    mu0: tuple = (0.2, 0.45)
+    U: tuple = (1.5, 2.5)
+
+    @property
+    def T(self):
+        return 2 * np.pi / self.w0
+
+    @property
+    def dt(self):
+        return self.T / 4096 * (1 + 1e-12)
+
+    def omegas(self):
+        return np.array([(i if i <= self.Nw // 2 - 1 else i - self.Nw) * self.w0 for i in range(self.Nw)])
+
+    def points(self, count: int, seed: int):
+        rng = np.random.default_rng(seed)
+        return [(float(rng.uniform(*self.mu0)), float(rng.uniform(*self.U))) for _ in range(count)]
+
+    def operator(self, pt):
+        mu0, U = pt
+        nu = U + 0.2j
+        A = synth.gl_stretched(self.N, mu0, nu=nu)
+        beta = max(0.0, synth.gl_rightmost(self.N, mu0, nu=nu) + 0.05)
+        return A, beta
+
+    def params(self, rsvdt, q: int, beta: float, precision: int):
+        return rsvdt.default_params(k=self.k, q=q, Nw=self.Nw, w=self.w0, dt=self.dt, TransientLength=self.T,
+                                    DiscFlg=int(beta > 0), beta=beta, precision=precision, Display=0)
+
+
+def solve_batch(fam: Family, pts, q: int, precision: int, sketches=None, seed: int = 0):
+    """RSVD-Delta-t for every point as one batch; returns ([(U, V, S)], seconds).
+    Random sketches (seeded, CN(0,1)) unless `sketches` are given."""
+    import rsvdt
+
+    b = rsvdt.Batch(precision)
+    for pt in pts:
+        A, beta = fam.operator(pt)
+        b.add(fam.params(rsvdt, q, beta, precision), A)
+    for i in range(len(pts)):
+        F = sketches[i] if sketches is not None else synth.complex_normal(fam.N, fam.k * fam.Nw, seed + i)
+        b.set_sketch(i, F)
+    t0 = time.perf_counter()
+    b.run()
+    out = [b.get_results(i) for i in range(len(pts))]
+    dt = time.perf_counter() - t0
+    b.close()
+    return out, dt
+
+
+def _phase_fix(C: np.ndarray) -> np.ndarray:
+    """Rotates each column so that its largest coefficient is real positive."""
+    idx = np.argmax(np.abs(C), axis=0)
+    ph = C[idx, np.arange(C.shape[1])]
+    return C * (np.abs(ph) / np.where(ph == 0, 1, ph))[None, :]
+
+
+class LearnedSketch:
+    def __init__(self, fam: Family, r: int = 64, hidden: int = 256, depth: int = 4, seed: int = 0):
+        self.fam = fam
+        self.r = r
+        self.widths = [3] + [hidden] * depth + [2 * r * fam.k]
+        self.seed = seed
+        self.net = None
+        self.Phi = None
+
+    def _inputs(self, pts):
+        f = self.fam
+        om = f.omegas()
+        rows = []
+        for mu0, U in pts:
+            for w in om:
+                rows.append([2 * (mu0 - f.mu0[0]) / (f.mu0[1] - f.mu0[0]) - 1,
+                             2 * (U - f.U[0]) / (f.U[1] - f.U[0]) - 1,
+                             w / (f.w0 * f.Nw / 2)])
+        return np.asarray(rows, dtype=np.float32)
+
+    def fit(self, pts, modes, steps: int = 3000, batch: int = 256, lr: float = 1e-3):
+        """modes: list of V (N x k*Nw, frequency-major) at the points."""
+        import rsvdt
+
+        f = self.fam
+        M = np.concatenate([V for V in modes], axis=1)  # N x (points * k * Nw)
+        G = M @ M.conj().T
+        ev, vec = np.linalg.eigh(G)
+        self.Phi = np.ascontiguousarray(vec[:, ::-1][:, :self.r])
+        self.pod_energy = float(ev[::-1][:self.r].sum() / ev.sum())
+        T = []
+        for V in modes:
+            for iw in range(f.Nw):
+                C = _phase_fix(self.Phi.conj().T @ V[:, iw * f.k:(iw + 1) * f.k])
+                T.append(np.concatenate([C.real.ravel(), C.imag.ravel()]))
+        T = np.asarray(T, dtype=np.float64)
+        self.t_mean = T.mean(axis=0)
+        self.t_std = T.std(axis=0) + 1e-12
+        Tn = ((T - self.t_mean) / self.t_std).astype(np.float32)
+        X = self._inputs(pts)
+        self.net = rsvdt.Mlp(self.widths, seed=self.seed)
+        t0 = time.perf_counter()
+        self.final_loss = self.net.train(X, Tn, batch=batch, steps=steps, lr=lr, seed=self.seed)
+        self.train_seconds = time.perf_counter() - t0
+        return self.final_loss
+
+    def sketch(self, pt) -> np.ndarray:
+        f = self.fam
+        Y = self.net.forward(self._inputs([pt])).astype(np.float64) * self.t_std + self.t_mean
+        F = np.zeros((f.N, f.k * f.Nw), dtype=np.complex128, order="F")
+        rk = self.r * f.k
+        for iw in range(f.Nw):
+            C = (Y[iw, :rk] + 1j * Y[iw, rk:]).reshape(self.r, f.k)
+            F[:, iw * f.k:(iw + 1) * f.k] = self.Phi @ C
+        return F
+
+
+def gain_check(fam: Family, pt, result, jmax: int = 3):
+    """max over frequencies and j < jmax of | |R v_j| - s_j | / s_j, with R v
+    from one complex128 direct action on the computed forcing modes."""
+    import rsvdt
+
+    U, V, S = result
+    A, beta = fam.operator(pt)
+    ctx = rsvdt.Context(fam.params(rsvdt, 0, beta, rsvdt.PREC_C128))
+    ctx.set_operator(A)
+    ctx.set_sketch(V)
+    ctx.action(rsvdt.DIRECT)
+    Y = ctx.get_block()
+    ctx.close()
+    k = fam.k
+    worst = 0.0
+    for iw in range(fam.Nw):
+        for j in range(min(jmax, k)):
+            s = S[j, iw]
+            worst = max(worst, abs(np.linalg.norm(Y[:, iw * k + j]) - s) / s)
+    return worst
+
+
+def gain_errors(results, refs, jmax: int = 3):
+    """Per problem: max over frequencies of the relative error of s_1, and of
+    s_j for j < jmax."""
+    e1, ej = [], []
+    for (_, _, S), (_, _, Sr) in zip(results, refs):
+        e1.append(float((np.abs(S[0] - Sr[0]) / Sr[0]).max()))
+        ej.append(float((np.abs(S[:jmax] - Sr[:jmax]) / Sr[:jmax]).max()))
+    return np.asarray(e1), np.asarray(ej)
