@@ -300,11 +300,15 @@ def learned_form(n_train: int = 200, n_held: int = 50, N: int = 2000, seed: int 
         e1, e3 = learned.gain_errors(r, ref)
         out[name] = {"solve_s": round(t, 3), "gain1_err_median": float(np.median(e1)), "gain1_err_max": float(e1.max()),
                      "gain_j<=3_err_median": float(np.median(e3)), "within_1e-3": int((e3 <= 1e-3).sum())}
-        if name == "learned_q0":
-            checks = [learned.gain_check(fam, p, rr) for p, rr in zip(held, r)]
-            out[name]["inference_s"] = round(t_inf, 3)
-            out[name]["fallbacks"] = int(sum(c > 1e-3 for c in checks))
+        if name in ("learned_q0", "random_q1"):
+            # FP64 check of the leading forcing mode: | |R v_1| - s_1 | / s_1,
+            # worst frequency; the learned run falls back above 1e-3.
+            checks = [learned.gain_check(fam, p, rr, jmax=1) for p, rr in zip(held, r)]
             out[name]["gain_check_median"] = float(np.median(checks))
+            out[name]["gain_check_over_1e-3"] = int(sum(c > 1e-3 for c in checks))
+            if name == "learned_q0":
+                out[name]["inference_s"] = round(t_inf, 3)
+                out[name]["fallbacks"] = out[name]["gain_check_over_1e-3"]
     return out
 
 

@@ -41,6 +41,9 @@ class Family:
     w0: float = 0.1
     mu0: tuple = (0.2, 0.45)
     U: tuple = (1.5, 2.5)
+    # Discounting places the leading eigenvalue at -margin (or lower): with
+    # one transient period the transient left is exp(-margin T) = 3.5e-6.
+    margin: float = 0.2
 
     @property
     def T(self):
@@ -61,7 +64,7 @@ class Family:
         mu0, U = pt
         nu = U + 0.2j
         A = synth.gl_stretched(self.N, mu0, nu=nu)
-        beta = max(0.0, synth.gl_rightmost(self.N, mu0, nu=nu) + 0.05)
+        beta = max(0.0, synth.gl_rightmost(self.N, mu0, nu=nu) + self.margin)
         return A, beta
 
     def params(self, rsvdt, q: int, beta: float, precision: int):
