@@ -1,0 +1,117 @@
+"""The C drop-in driver for the reference's main.c (bin/rsvdt_main):
+variables.yaml keys, defaults and errors of SourceCode/ReadUserInput.c,
+PETSc-binary inputs and the results folder of SourceCode/SaveResults.c."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from rsvdt import petsc_io, synth
+
+
+@pytest.fixture(scope="module")
+def driver(built_lib):
+    from rsvdt import build
+    path = build.build_host()
+    assert path and os.path.exists(path)
+    return path
+
+
+def write_yaml(path, **keys):
+    with open(path, "w") as f:
+        f.write("# generated for a test\n")
+        for k, v in keys.items():
+            f.write(f"{k}: {v}   # comment\n")
+
+
+BASE = dict(RootDir="ROOT/", ResultsDir="", OperatorDir="A", k=2, q=0, Nw=8, w=0.1, TwoPI="false",
+            TransientLength=62.83185307179586, dt=0.15, TransientRemoval="false", Display=0,
+            TransICDir="ic", RandSeed=5)
+
+
+def run(driver, tmp_path, **keys):
+    cfg = dict(BASE)
+    cfg.update(keys)
+    cfg = {k: v for k, v in cfg.items() if v is not None}
+    if cfg.get("RootDir") == "ROOT/":
+        cfg["RootDir"] = str(tmp_path) + "/"
+    y = tmp_path / "variables.yaml"
+    write_yaml(y, **cfg)
+    return subprocess.run([driver, "-inputs", str(y)], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+
+
+@pytest.mark.parametrize("missing,message", [
+    ("TransientLength", "Must specify 'TransientLength'"),
+    ("dt", "Must specify 'dt'"),
+    ("w", "Must specify 'dt'"),  # the reference's message for a missing w (SourceCode/ReadUserInput.c:28)
+    ("RootDir", "Must specify 'RootDir'"),
+    ("OperatorDir", "Must specify 'OperatorDir'"),
+    ("Nw", "Must specify 'Nw'"),
+    ("TransICDir", "Must specify 'TransICDir'"),
+])
+def test_required_keys(driver, tmp_path, missing, message):
+    r = run(driver, tmp_path, **{missing: None})
+    assert r.returncode != 0
+    assert message in r.stderr
+
+
+def test_flag_requires_directory_and_bad_values(driver, tmp_path):
+    r = run(driver, tmp_path, InputForcingFlg="true")
+    assert r.returncode != 0 and "Must specify 'InputForcingDir'" in r.stderr
+    r = run(driver, tmp_path, k="1.5")
+    assert r.returncode != 0 and "no integer value" in r.stderr
+    r = run(driver, tmp_path, TwoPI="maybe")
+    assert r.returncode != 0 and "Unknown logical value" in r.stderr
+    r = run(driver, tmp_path, DiscFlg="true")
+    assert r.returncode != 0 and "specify 'beta'" in r.stderr
+    r = run(driver, tmp_path, TransRun="true")
+    assert r.returncode != 0 and "TransRun" in r.stderr
+
+
+def test_defaults_are_announced(driver, tmp_path):
+    r = run(driver, tmp_path, k=None, q=None)
+    out = r.stdout
+    assert "Setting 'k' to default value: 3" in out
+    assert "Setting 'q' to default value: 0" in out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("opt", [1, 2])
+def test_end_to_end_matches_the_library(driver, tmp_path, opt):
+    import rsvdt
+    A = synth.gl_operator(64, mu0=0.2)
+    petsc_io.write_mat(str(tmp_path / "A"), A)
+    k, nw = 2, 8
+    F = synth.complex_normal(64, k * nw, 9)
+    petsc_io.write_mat(str(tmp_path / "F"), F)
+    r = run(driver, tmp_path, InputForcingFlg="true", InputForcingDir="F", q=1, SaveResultsOpt=opt)
+    assert r.returncode == 0, r.stderr + r.stdout
+    folder = tmp_path / "ResolventModes_0"
+    S = petsc_io.read_mat(str(folder / "S_hat")).toarray()
+    assert S.shape == (k, nw)
+    ctx = rsvdt.Context(rsvdt.default_params(k=k, q=1, Nw=nw, w=0.1, dt=0.15, TransientLength=BASE["TransientLength"],
+                                             Display=0))
+    ctx.set_operator(A)
+    ctx.set_sketch(F)
+    ctx.run()
+    U, V, Sr = ctx.get_results()
+    ctx.close()
+    assert np.abs(S.real - Sr).max() <= 1e-12 * Sr.max() and np.abs(S.imag).max() == 0
+    if opt == 1:
+        for ik in range(k):
+            Uk = petsc_io.read_mat(str(folder / f"U_hat_k{ik + 1}_allFreqs")).toarray()
+            Vk = petsc_io.read_mat(str(folder / f"V_hat_k{ik + 1}_allFreqs")).toarray()
+            assert Uk.shape == (64, nw) and Vk.shape == (64, nw)
+            assert np.allclose(Uk, U[:, [iw * k + ik for iw in range(nw)]], atol=1e-14)
+            assert np.allclose(Vk, V[:, [iw * k + ik for iw in range(nw)]], atol=1e-14)
+    else:
+        for iw in range(nw):
+            Uw = petsc_io.read_mat(str(folder / f"U_hat_Freq{iw}_allK")).toarray()
+            assert Uw.shape == (64, k)
+            assert np.allclose(Uw, U[:, iw * k:(iw + 1) * k], atol=1e-14)
+    assert (folder / "variables.yaml").exists()
+    # A second run goes to the next folder (SourceCode/CreateResultsDir.c:21-27).
+    r = run(driver, tmp_path, InputForcingFlg="true", InputForcingDir="F", q=0, SaveResultsOpt=opt)
+    assert r.returncode == 0
+    assert (tmp_path / "ResolventModes_1" / "S_hat").exists()
