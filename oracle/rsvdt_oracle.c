@@ -162,8 +162,9 @@ static void build_idft(int64_t Nw_eff, int64_t Ns, int real_op, zc *idft) {
 
 static void build_dft(int64_t Nw, int64_t Nw_eff, int real_op, zc *dft) {
   /* SourceCode/CreateDFTiDFTMats.c:61-85: dft[j, iw] = exp(alpha*iw*j),
-   * alpha = -2*pi*i/Nw (-2*pi*i/(2Nw) for a real operator). */
-  double alpha_im = real_op ? -2 * ORC_PI / (double)(2 * Nw) : -2 * ORC_PI / (double)Nw;
+   * alpha = -2*pi*i/Nw_eff (-2*pi*i/(2 Nw_eff) for a real operator): the
+   * `Nw` of that formula is the column count of idft (line 26). */
+  double alpha_im = real_op ? -2 * ORC_PI / (double)(2 * Nw_eff) : -2 * ORC_PI / (double)Nw_eff;
   for (int64_t iw = 0; iw < Nw_eff; ++iw) {
     double v_im = alpha_im * (double)iw;
     for (int64_t j = 0; j < Nw; ++j) {

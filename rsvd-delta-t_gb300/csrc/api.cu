@@ -214,8 +214,16 @@ static rsvdt_status setup_grid_and_tables(rsvdt_ctx *ctx) {
       tab32[(size_t)(it * Nwe + iw)] = zmake<z64>((float)e.re, (float)e.im);
     }
   }
+  // The reference's `Nw` in this formula is the column count of idft, i.e.
+  // Nw_eff (SourceCode/CreateDFTiDFTMats.c:26): alpha = -2 pi i / (2 Nw_eff)
+  // for a real operator, -2 pi i / Nw_eff otherwise; its sample vector J has
+  // 2 Nw_eff (real) or Nw_eff entries, which must equal the Nw snapshot rows
+  // (an odd Nw with a real operator is a size mismatch there, and an error
+  // here).
+  if (ctx->real_op && 2 * Nwe != Nw)
+    return set_err(ctx, RSVDT_ERR_ARG, "a real-valued operator needs an even Nw (Nw = %lld)", (long long)Nw);
   std::vector<z128> dft((size_t)Nwe * Nw);
-  const double a_dft = ctx->real_op ? -2 * kPi / (double)(2 * Nw) : -2 * kPi / (double)Nw;
+  const double a_dft = ctx->real_op ? -2 * kPi / (double)(2 * Nwe) : -2 * kPi / (double)Nwe;
   for (int64_t iw = 0; iw < Nwe; ++iw) {
     const double v_im = a_dft * (double)iw;
     for (int64_t j = 0; j < Nw; ++j) {

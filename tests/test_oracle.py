@@ -66,6 +66,24 @@ def test_direct_action_is_the_resolvent_up_to_a_phase():
         assert np.linalg.norm(Y[:, iw] - ph * x) / np.linalg.norm(x) < 1e-4
 
 
+def test_real_operator_action_is_the_resolvent_up_to_a_phase():
+    """A real-valued operator keeps the Nw/2 non-negative frequencies; the
+    DFT over the Nw snapshots of one period then picks frequency iw * w
+    (SourceCode/CreateDFTiDFTMats.c:79, alpha = -2 pi i / (2 Nw_eff))."""
+    A = synth.gl_operator(64, nu=2.0, gamma=1.0, mu0=0.2)
+    w, Nw, dt, T = 0.1, 16, 0.15, 2 * np.pi / 0.1
+    o = oracle.Oracle(A, Nw, w, dt, T, transient_removal=True)
+    assert o.real_op and o.Nw_eff == Nw // 2
+    F = synth.complex_normal(64, Nw // 2, 13)
+    Y = o.ts_action(1, F)
+    Ad = A.toarray()
+    for iw in range(Nw // 2):
+        om = oracle.freq_of(iw, Nw, w, real_op=True)
+        x = np.linalg.solve(1j * om * np.eye(64) - Ad, F[:, iw])
+        ph = np.exp(1j * om * (o.Nt + o.R) * o.dt)
+        assert np.linalg.norm(Y[:, iw] - ph * x) / np.linalg.norm(x) < 1e-4, iw
+
+
 def test_adjoint_action_is_the_adjoint_resolvent_up_to_a_phase():
     A, w, Nw, dt, T = _small()
     o = oracle.Oracle(A, Nw, w, dt, T, transient_removal=True)
