@@ -193,6 +193,60 @@ rsvdt_status rsvdt_rk4_advance(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_
 rsvdt_status rsvdt_rk4_profile(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps,
                                double *stage_ms);
 
+/* ------------------------------------------------------ transient simulation
+ * The initial-value problem dq/dt = A q (A discounted when DiscFlg) by
+ * unforced RK4 from a given initial vector, with the norm checked every
+ * save_mod steps. Replaces SourceCode/TransientRunRK4.c:11-228 with
+ * SourceCode/TSTransRK4.c:5-40 and SourceCode/TransientRemovalEst.c:6-129
+ * (the file writing stays with the caller, through the callbacks). */
+typedef struct {
+  int64_t periods;     /* TransPeriods: integrate periods * Nt_period steps */
+  int64_t save_mod;    /* TransSaveMod (>= 1): norm checked every save_mod steps */
+  double div_val;      /* TransDivVal: stop when the norm exceeds it */
+  double con_val;      /* TransConVal: stop when the norm falls below it */
+  int32_t save;        /* TransSave: pass every checked snapshot to on_snapshot */
+  int32_t removal_est; /* TransRemovalEst: transient-removal estimate every period */
+} rsvdt_trans_params;
+
+typedef enum {
+  RSVDT_TRANS_DONE = 0,      /* all steps taken */
+  RSVDT_TRANS_NAN = 1,       /* a checked norm was NaN */
+  RSVDT_TRANS_DIVERGED = 2,  /* a checked norm exceeded div_val */
+  RSVDT_TRANS_CONVERGED = 3  /* a checked norm fell below con_val */
+} rsvdt_trans_stop;
+
+typedef struct {
+  double dt;          /* T/Nw / ceil((T/Nw) / dt_grid) (TransientRunRK4.c:42) */
+  int64_t Nt_period;  /* round(T / dt) */
+  int64_t rend;       /* Nt_period * periods */
+  int64_t n_saved;    /* floor(rend / save_mod) + 1: length of `norms` */
+  int64_t steps;      /* steps taken */
+  int32_t stop;       /* rsvdt_trans_stop */
+  double last_norm;   /* norm at the stop (or at the last check) */
+} rsvdt_trans_info;
+
+/* Called with snapshot number pos (= step / save_mod, 0 for the initial
+ * vector) and the N complex values of the state; nonzero aborts the run
+ * with RSVDT_ERR_IO. */
+typedef int (*rsvdt_trans_snapshot_fn)(void *user, int64_t pos, const double *q, int64_t n);
+/* Called at the end of every period p >= 1 with the Nw/2 initial and
+ * updated transient norms of TransientRemovalEst; nonzero aborts. */
+typedef int (*rsvdt_trans_estimate_fn)(void *user, int64_t period, const double *initial,
+                                       const double *updated, int64_t count);
+
+/* Time grid of a transient run (info->dt, Nt_period, rend, n_saved) without
+ * running it. */
+rsvdt_status rsvdt_trans_grid(rsvdt_ctx *ctx, const rsvdt_trans_params *tp, rsvdt_trans_info *info);
+
+/* Runs the transient simulation. q: N complex values, the initial vector on
+ * entry and the last snapshot on return. norms: n_saved doubles, zeroed
+ * then filled at every check that passed (norms[0] = |q0|). Callbacks may be
+ * NULL. A stop on NaN / divergence / convergence is not an error: it is
+ * reported in info->stop, as the reference prints it and saves what it has. */
+rsvdt_status rsvdt_trans_run(rsvdt_ctx *ctx, const rsvdt_trans_params *tp, double *q, double *norms,
+                             rsvdt_trans_snapshot_fn on_snapshot, rsvdt_trans_estimate_fn on_estimate,
+                             void *user, rsvdt_trans_info *info);
+
 /* ---------------------------------------------------------------- batching
  * Many independent problems of uneven size (own operator, k, Nw, time
  * grid, q) solved together: every action of the sequence runs for all

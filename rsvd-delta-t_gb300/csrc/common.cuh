@@ -203,6 +203,8 @@ bool launch_batched_step(cudaStream_t st, int prec, const void *args, const int2
 void launch_set_step(cudaStream_t st, int64_t *step, int64_t i);
 rsvdt_status launch_unforced_steps(rsvdt_ctx *ctx, int dir, z128 *cols, int64_t ncols,
                                    int64_t nsteps);
+rsvdt_status launch_trans_steps(rsvdt_ctx *ctx, double dt, z128 *y, z128 *work, int64_t nsteps,
+                                cudaGraphExec_t *graph);
 // dense.cu
 rsvdt_status launch_colmajor_to_blk(rsvdt_ctx *ctx, const z128 *src, int64_t rows, int64_t ld,
                                     int64_t C, z128 *dst);

@@ -779,6 +779,9 @@ template <class Z>
 static void launch_stage(int stage, const StepArgs<Z> &P, cudaStream_t st) {
   if (P.bs == 5) {
     switch (P.K) {
+      case 1:  // a single state vector (transient simulation), complex128 rows
+        if constexpr (sizeof(Z) == 16) return launch_bstage<Z, 1>(stage, P, st);
+        break;
       case 2: return launch_bstage<Z, 2>(stage, P, st);
       case 4: return launch_bstage<Z, 4>(stage, P, st);
       case 6: return launch_bstage<Z, 6>(stage, P, st);
@@ -983,6 +986,50 @@ rsvdt_status launch_unforced_steps(rsvdt_ctx *ctx, int dir, z128 *cols, int64_t 
   for (int64_t s = 0; s < nsteps; ++s) enqueue_step(ctx, P);
   ctx->launches += 4 * nsteps;
   if (!cuda_ok(ctx, cudaGetLastError(), "unforced steps")) return RSVDT_ERR_CUDA;
+  return RSVDT_OK;
+}
+
+// Unforced RK4 (SourceCode/TSTransRK4.c:15-36) of one complex128 state
+// vector y with time step dt, for the transient simulation
+// (SourceCode/TransientRunRK4.c:128-130). work holds zA, zB, acc, F2, F3
+// (5 N values); F2 and F3 must be zero (no forcing writes them). Full
+// groups of kGraphSteps steps replay a CUDA graph cached in *graph, which
+// the caller destroys.
+rsvdt_status launch_trans_steps(rsvdt_ctx *ctx, double dt, z128 *y, z128 *work, int64_t nsteps,
+                                cudaGraphExec_t *graph) {
+  const int64_t N = ctx->N;
+  auto P = make_args<z128>(ctx, 1, false);
+  P.K = 1;
+  P.y = y;
+  P.zA = work;
+  P.zB = work + N;
+  P.acc = work + 2 * N;
+  P.F2 = work + 3 * N;
+  P.F3 = work + 4 * N;
+  P.ring = nullptr;
+  P.dt = dt;
+  P.dt_2 = dt / 2;
+  P.dt_6 = dt / 6;
+  P.dt_62 = dt / 6 * 2;
+  int64_t done = 0;
+  if (nsteps >= kGraphSteps) {
+    if (!*graph) {
+      cudaGraph_t g;
+      if (!cuda_ok(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal),
+                   "begin capture"))
+        return RSVDT_ERR_CUDA;
+      for (int64_t s = 0; s < kGraphSteps; ++s) enqueue_step(ctx, P);
+      if (!cuda_ok(ctx, cudaStreamEndCapture(ctx->stream, &g), "end capture")) return RSVDT_ERR_CUDA;
+      const cudaError_t e = cudaGraphInstantiate(graph, g, 0);
+      cudaGraphDestroy(g);
+      if (!cuda_ok(ctx, e, "graph instantiate")) return RSVDT_ERR_CUDA;
+    }
+    for (; done + kGraphSteps <= nsteps; done += kGraphSteps)
+      if (!cuda_ok(ctx, cudaGraphLaunch(*graph, ctx->stream), "graph launch")) return RSVDT_ERR_CUDA;
+  }
+  for (; done < nsteps; ++done) enqueue_step(ctx, P);
+  ctx->launches += 4 * nsteps;
+  if (!cuda_ok(ctx, cudaGetLastError(), "transient steps")) return RSVDT_ERR_CUDA;
   return RSVDT_OK;
 }
 

@@ -229,3 +229,24 @@ int pb_write_dense_real(const char *path, const double *a, int64_t rows, int64_t
                         int errlen) {
   return write_dense_impl(path, a, rows, cols, ld, 0, err, errlen);
 }
+
+int pb_write_vec(const char *path, const double *v, int64_t n, int is_complex, char *err, int errlen) {
+  FILE *f = fopen(path, "wb");
+  if (!f) return fail(err, errlen, "cannot create %s", path);
+  unsigned char h[16];
+  put64(h, VEC_CLASSID);
+  put64(h + 8, (uint64_t)n);
+  int ok = fwrite(h, 1, 16, f) == 16;
+  unsigned char e[16];
+  for (int64_t i = 0; i < n && ok; ++i) {
+    double re = is_complex ? v[2 * i] : v[i], im = is_complex ? v[2 * i + 1] : 0.0;
+    uint64_t u;
+    memcpy(&u, &re, 8);
+    put64(e, u);
+    memcpy(&u, &im, 8);
+    put64(e + 8, u);
+    ok = fwrite(e, 1, 16, f) == 16;
+  }
+  if (fclose(f) != 0) ok = 0;
+  return ok ? 0 : fail(err, errlen, "write error on %s", path);
+}

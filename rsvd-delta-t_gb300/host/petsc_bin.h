@@ -28,5 +28,9 @@ int pb_write_dense(const char *path, const double *a, int64_t rows, int64_t cols
  * imaginary parts, the layout of the reference's complex build). */
 int pb_write_dense_real(const char *path, const double *a, int64_t rows, int64_t cols, int64_t ld,
                         char *err, int errlen);
+/* Writes a Vec of n complex values (is_complex = 1, 2n doubles) or of n
+ * real values stored as complex with zero imaginary parts, with a 64-bit
+ * length, as VecView does (SourceCode/TransientRunRK4.c:117-119). */
+int pb_write_vec(const char *path, const double *v, int64_t n, int is_complex, char *err, int errlen);
 
 #endif

@@ -11,16 +11,20 @@
  * RSVD-Delta-t sequence through the C ABI (include/rsvdt.h) and writes the
  * same outputs into RootDir + ResultsDir + ResolventModes_<n>/
  * (SourceCode/CreateResultsDir.c:20-30, SourceCode/SaveResults.c:32-92).
- * The transient simulation mode (TransRun: true) is not part of this build
- * and exits with an error.
+ * With TransRun: true it runs the transient simulation instead
+ * (SourceCode/main.c:119-124, SourceCode/TransientRunRK4.c:11-228) and
+ * writes its snapshots and norms into RootDir + ResultsDir +
+ * TransientSnapshots_<n>/.
  */
 #include <ctype.h>
 #include <errno.h>
+#include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <sys/stat.h>
+#include <time.h>
 #include <unistd.h>
 
 #include "petsc_bin.h"
@@ -149,6 +153,10 @@ static void warn_default_i(const char *key, long long v) {
   printf("Warning: '%s' variable not found. Setting '%s' to default value: %lld\n", key, key, v);
 }
 
+static void warn_default_g(const char *key, double v) {
+  printf("Warning: '%s' variable not found. Setting '%s' to default value: %g\n", key, key, v);
+}
+
 typedef struct {
   char root[PATHLEN], results[PATHLEN], op[PATHLEN], forcing[PATHLEN];
   char wdir[5][PATHLEN];
@@ -156,6 +164,10 @@ typedef struct {
   int wflag[5];
   int input_forcing, trans_run, save_opt;
   int64_t rand_seed;
+  /* Transient simulation (SourceCode/Variables.h TransRun_vars). */
+  int trans_ic_flg;
+  char icdir[PATHLEN];
+  rsvdt_trans_params tp;
 } drv_t;
 
 static void join(char *out, const char *a, const char *b) {
@@ -238,10 +250,45 @@ static void read_user_input(rsvdt_params *p, drv_t *d) {
   if (!set && p->DiscFlg) die("Discounting flag is on! Either set Discounting to zero or specify 'beta'");
   p->beta = set ? r : 0.0;
   if (p->beta < 0 && p->DiscFlg) die("'beta' must be positive, current value: %g", p->beta);
-  int ic;
-  char icdir[PATHLEN];
-  set = get_bool("TransICFlg", &ic);
-  if (!(!set && d->trans_run) && !get_str("TransICDir", icdir)) die("Must specify 'TransICDir'");
+  /* SourceCode/ReadUserInput.c:134-171: the transient-run keys get their
+   * defaults (and warnings) only when TransRun is on; TransICDir is required
+   * unless TransICFlg is absent in a transient run. */
+  set = get_bool("TransICFlg", &d->trans_ic_flg);
+  if (!set && d->trans_run) {
+    d->trans_ic_flg = 0;
+    warn_default_i("TransICFlg", 0);
+  } else if (!get_str("TransICDir", d->icdir)) {
+    die("Must specify 'TransICDir'");
+  }
+  rsvdt_trans_params *tp = &d->tp;
+  b = 0;
+  if (!get_real("TransDivVal", &tp->div_val) && d->trans_run) {
+    tp->div_val = 1e3;
+    warn_default_g("TransDivVal", tp->div_val);
+  }
+  if (!get_real("TransConVal", &tp->con_val) && d->trans_run) {
+    tp->con_val = 1e-8;
+    warn_default_g("TransConVal", tp->con_val);
+  }
+  if (!get_bool("TransSave", &b) && d->trans_run) {
+    b = 0;
+    warn_default_i("TransSave", 0);
+  }
+  tp->save = b;
+  b = 0;
+  if (!get_bool("TransRemovalEst", &b) && d->trans_run) {
+    b = 0;
+    warn_default_i("TransRemovalEst", 0);
+  }
+  tp->removal_est = b;
+  if (!get_int("TransSaveMod", &tp->save_mod) && d->trans_run) {
+    tp->save_mod = 100;
+    warn_default_i("TransSaveMod", 100);
+  }
+  if (!get_int("TransPeriods", &tp->periods) && d->trans_run) {
+    tp->periods = 1;
+    warn_default_i("TransPeriods", 1);
+  }
   printf("\n");
 }
 
@@ -265,6 +312,130 @@ static void load_csr(const char *path, pb_csr *m) {
   if (pb_read_mat(path, m, err, sizeof err)) die("%s", err);
 }
 
+/* SaveInputVarsCopy (SourceCode/SaveInputVarsCopy.c:26-38). */
+static void save_inputs_copy(const char *inputs, const char *folder) {
+  char path[PATHLEN];
+  const char *base = strrchr(inputs, '/');
+  base = base ? base + 1 : inputs;
+  join(path, folder, base);
+  FILE *src = fopen(inputs, "rb"), *dst = fopen(path, "wb");
+  if (!src || !dst) die("cannot copy %s to %s", inputs, path);
+  char buf[1024];
+  size_t n;
+  while ((n = fread(buf, 1, sizeof buf, src)) > 0) fwrite(buf, 1, n, dst);
+  fclose(src);
+  fclose(dst);
+}
+
+/* Uniform [0,1) real and imaginary parts, then normalised: the
+ * distribution of VecSetRandom + VecNormalize in
+ * SourceCode/TransientRunRK4.c:88-93, from a splitmix64 stream seeded by
+ * RandSeed (PETSc's own generator is not reproduced). */
+static void random_ic(double *q, int64_t n, uint64_t seed) {
+  uint64_t x = seed;
+  double s = 0;
+  for (int64_t i = 0; i < 2 * n; ++i) {
+    uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    q[i] = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+    s += q[i] * q[i];
+  }
+  s = sqrt(s);
+  for (int64_t i = 0; i < 2 * n; ++i) q[i] /= s;
+}
+
+typedef struct {
+  const char *folder;
+  char err[512];
+} trans_io;
+
+static int write_snapshot(void *user, int64_t pos, const double *q, int64_t n) {
+  trans_io *io = (trans_io *)user;
+  char path[PATHLEN], name[64];
+  snprintf(name, sizeof name, "q_transient_%d", (int)pos);
+  join(path, io->folder, name);
+  return pb_write_vec(path, q, n, 1, io->err, sizeof io->err);
+}
+
+static int write_estimate(void *user, int64_t period, const double *initial, const double *updated,
+                          int64_t count) {
+  trans_io *io = (trans_io *)user;
+  char path[PATHLEN], name[96];
+  snprintf(name, sizeof name, "Initial_transient_norm_period_%d", (int)period);
+  join(path, io->folder, name);
+  if (pb_write_vec(path, initial, count, 0, io->err, sizeof io->err)) return 1;
+  snprintf(name, sizeof name, "Updated_transient_norm_period_%d", (int)period);
+  join(path, io->folder, name);
+  return pb_write_vec(path, updated, count, 0, io->err, sizeof io->err);
+}
+
+/* PreProcessing for a transient run (SourceCode/PreProcessing.c:34-67:
+ * no weights, no sketch) and TransientRunRK4
+ * (SourceCode/TransientRunRK4.c:32-224). */
+static int transient_run(rsvdt_params *p, drv_t *d, const char *inputs) {
+  rsvdt_ctx *ctx = NULL;
+  rsvdt_status st = rsvdt_create(p, &ctx);
+  if (st != RSVDT_OK) die("%s", ctx ? rsvdt_last_error(ctx) : "context creation failed");
+  char path[PATHLEN], err[512];
+  pb_csr A;
+  join(path, d->root, d->op);
+  printf("Loading the operator: %s \n", path);
+  load_csr(path, &A);
+  if (A.rows != A.cols) die("the operator must be square, current size = %lld x %lld", (long long)A.rows,
+                            (long long)A.cols);
+  check(ctx, rsvdt_set_operator(ctx, A.rows, A.rowptr, A.col, A.val), "operator");
+  printf("The operator is loaded (N = %lld)\n", (long long)A.rows);
+  const int64_t N = A.rows;
+  pb_free(&A);
+  create_results_dir(d, "TransientSnapshots_");
+
+  printf("\n********************************************\n************** Transient run ***************\n"
+         "********************************************\n\n");
+  rsvdt_trans_info info;
+  check(ctx, rsvdt_trans_grid(ctx, &d->tp, &info), "transient grid");
+  if (d->tp.save)
+    printf("Total snapshots to be saved = %d\n", (int)info.n_saved);
+  else
+    printf("Saving snapshots is not requested\n");
+  double *q = (double *)malloc(sizeof(double) * 2 * (size_t)N);
+  double *norms = (double *)calloc((size_t)info.n_saved, sizeof(double));
+  if (!q || !norms) die("out of memory");
+  if (d->trans_ic_flg) {
+    printf("Reading the initial vector\n");
+    if (snprintf(path, PATHLEN, "%s%s%s", d->root, d->results, d->icdir) >= PATHLEN) die("path too long");
+    double *v = NULL;
+    int64_t n = 0;
+    if (pb_read_vec(path, &v, &n, err, sizeof err)) die("%s", err);
+    if (n != N) die("the initial vector has %lld entries, the operator %lld rows", (long long)n, (long long)N);
+    memcpy(q, v, sizeof(double) * 2 * (size_t)N);
+    free(v);
+  } else {
+    printf("Random vector is generated\n\n");
+    random_ic(q, N, (uint64_t)d->rand_seed);
+  }
+  trans_io io;
+  io.folder = d->folder;
+  io.err[0] = '\0';
+  const time_t t0 = time(NULL);
+  st = rsvdt_trans_run(ctx, &d->tp, q, norms, write_snapshot, write_estimate, &io, &info);
+  if (st != RSVDT_OK) die("transient run: %s%s%s", rsvdt_last_error(ctx), io.err[0] ? ": " : "", io.err);
+  const int el = (int)difftime(time(NULL), t0);
+  printf("*** Transient simulation elapsed time = %02d:%02d:%02d ***\n", el / 3600, (el / 60) % 60, el % 60);
+  printf("\nThe results directory is: %s\n\n", d->folder);
+  join(path, d->folder, "q_transient_norms");
+  if (pb_write_vec(path, norms, info.n_saved, 0, err, sizeof err)) die("%s", err);
+  join(path, d->folder, "q_transient_last_snapshot");
+  if (pb_write_vec(path, q, N, 1, err, sizeof err)) die("%s", err);
+  save_inputs_copy(inputs, d->folder);
+  printf("DONE :))\n\n");
+  free(q);
+  free(norms);
+  rsvdt_destroy(ctx);
+  return 0;
+}
+
 int main(int argc, char **argv) {
   const char *inputs = NULL;
   for (int a = 1; a + 1 < argc; ++a)
@@ -277,7 +448,7 @@ int main(int argc, char **argv) {
   drv_t d;
   memset(&d, 0, sizeof d);
   read_user_input(&p, &d);
-  if (d.trans_run) die("TransRun (the transient simulation mode) is not supported by this build");
+  if (d.trans_run) return transient_run(&p, &d, inputs);
 
   rsvdt_ctx *ctx = NULL;
   rsvdt_status st = rsvdt_create(&p, &ctx);
@@ -382,17 +553,7 @@ int main(int argc, char **argv) {
       if (pb_write_dense(path, V + 2 * iw * k * g.Nb, g.Nb, k, g.Nb, err, sizeof err)) die("%s", err);
     }
   }
-  /* SaveInputVarsCopy (SourceCode/SaveInputVarsCopy.c:26-38). */
-  const char *base = strrchr(inputs, '/');
-  base = base ? base + 1 : inputs;
-  join(path, d.folder, base);
-  FILE *src = fopen(inputs, "rb"), *dst = fopen(path, "wb");
-  if (!src || !dst) die("cannot copy %s to %s", inputs, path);
-  char buf[1024];
-  size_t n;
-  while ((n = fread(buf, 1, sizeof buf, src)) > 0) fwrite(buf, 1, n, dst);
-  fclose(src);
-  fclose(dst);
+  save_inputs_copy(inputs, d.folder);
   printf("DONE :))\n\n");
   free(U);
   free(V);

@@ -38,7 +38,7 @@ EXPORTED = [
     "rsvdt_qr_all_freqs", "rsvdt_svd_all_freqs", "rsvdt_power_iteration", "rsvdt_run",
     "rsvdt_get_results", "rsvdt_rk4_steps", "rsvdt_rk4_reset", "rsvdt_rk4_advance",
     "rsvdt_rk4_profile", "rsvdt_synchronize", "rsvdt_stream", "rsvdt_launch_count",
-    "rsvdt_qr_all_freqs_noalloc",
+    "rsvdt_qr_all_freqs_noalloc", "rsvdt_trans_grid", "rsvdt_trans_run",
     "rsvdt_batch_create", "rsvdt_batch_destroy", "rsvdt_batch_last_error", "rsvdt_batch_add",
     "rsvdt_batch_set_sketch", "rsvdt_batch_random_sketch", "rsvdt_batch_run", "rsvdt_batch_get_results",
     "rsvdt_batch_get_grid", "rsvdt_batch_get_tuning", "rsvdt_batch_launch_count",
@@ -76,6 +76,26 @@ class Grid(C.Structure):
         ("ResRatio", C.c_int64), ("Nw_eff", C.c_int64), ("N", C.c_int64), ("Nb", C.c_int64),
         ("Nc", C.c_int64),
     ]
+
+
+class TransParams(C.Structure):
+    _fields_ = [
+        ("periods", C.c_int64), ("save_mod", C.c_int64), ("div_val", C.c_double), ("con_val", C.c_double),
+        ("save", C.c_int32), ("removal_est", C.c_int32),
+    ]
+
+
+class TransInfo(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double), ("Nt_period", C.c_int64), ("rend", C.c_int64), ("n_saved", C.c_int64),
+        ("steps", C.c_int64), ("stop", C.c_int32), ("last_norm", C.c_double),
+    ]
+
+
+TRANS_DONE, TRANS_NAN, TRANS_DIVERGED, TRANS_CONVERGED = range(4)
+TRANS_SNAPSHOT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.c_int64)
+TRANS_ESTIMATE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                C.c_int64)
 
 
 class RsvdtError(RuntimeError):
@@ -123,6 +143,9 @@ def load_library(path: str | None = None) -> C.CDLL:
         "rsvdt_rk4_advance": (C.c_int, [vp, C.c_int, i64, i64]),
         "rsvdt_rk4_profile": (C.c_int, [vp, C.c_int, i64, i64, d]),
         "rsvdt_qr_all_freqs_noalloc": (C.c_int, [vp, vp, i64, i64, i64, vp, C.c_char_p, i64]),
+        "rsvdt_trans_grid": (C.c_int, [vp, P(TransParams), P(TransInfo)]),
+        "rsvdt_trans_run": (C.c_int, [vp, P(TransParams), d, d, TRANS_SNAPSHOT_FN, TRANS_ESTIMATE_FN, vp,
+                                      P(TransInfo)]),
         "rsvdt_batch_create": (C.c_int, [C.c_int32, P(vp)]),
         "rsvdt_batch_destroy": (None, [vp]),
         "rsvdt_batch_last_error": (C.c_char_p, [vp]),
@@ -325,6 +348,44 @@ class Context:
         self._check(self._lib.rsvdt_rk4_profile(self._h, direction, i0, nsteps,
                                                 out.ctypes.data_as(C.POINTER(C.c_double))))
         return out.tolist()
+
+    # -------------------------------------------------------- transient run
+    @staticmethod
+    def _trans_params(periods=1, save_mod=100, div_val=1e3, con_val=1e-8, save=False, removal_est=False):
+        # Defaults of SourceCode/ReadUserInput.c:142-171.
+        return TransParams(int(periods), int(save_mod), float(div_val), float(con_val), int(bool(save)),
+                           int(bool(removal_est)))
+
+    def trans_grid(self, **kw) -> TransInfo:
+        info = TransInfo()
+        tp = self._trans_params(**kw)
+        self._check(self._lib.rsvdt_trans_grid(self._h, C.byref(tp), C.byref(info)))
+        return info
+
+    def trans_run(self, q0: np.ndarray, **kw):
+        """Transient simulation from q0 (N complex). Returns (q_last, norms,
+        info, snapshots {pos: q}, estimates [(period, initial, updated)]);
+        snapshots are kept only with save=True."""
+        tp = self._trans_params(**kw)
+        info = TransInfo()
+        self._check(self._lib.rsvdt_trans_grid(self._h, C.byref(tp), C.byref(info)))
+        q = np.ascontiguousarray(q0, dtype=np.complex128).copy()
+        norms = np.zeros(info.n_saved)
+        snaps, ests = {}, []
+
+        def on_snap(_u, pos, ptr, n):
+            snaps[int(pos)] = np.ctypeslib.as_array(ptr, shape=(2 * n,)).view(np.complex128).copy()
+            return 0
+
+        def on_est(_u, period, pi, pu, count):
+            ests.append((int(period), np.ctypeslib.as_array(pi, shape=(count,)).copy(),
+                         np.ctypeslib.as_array(pu, shape=(count,)).copy()))
+            return 0
+
+        fs, fe = TRANS_SNAPSHOT_FN(on_snap), TRANS_ESTIMATE_FN(on_est)
+        self._check(self._lib.rsvdt_trans_run(self._h, C.byref(tp), _dptr(q.view(np.float64)), _dptr(norms), fs, fe,
+                                              None, C.byref(info)))
+        return q, norms, info, snaps, ests
 
     def synchronize(self) -> None:
         self._check(self._lib.rsvdt_synchronize(self._h))

@@ -24,7 +24,7 @@ MAIN_PATH = os.path.join(BIN_DIR, "rsvdt_main")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
-CU_SOURCES = ["api.cu", "step.cu", "dense.cu", "batch.cu", "mlp.cu"]
+CU_SOURCES = ["api.cu", "step.cu", "dense.cu", "batch.cu", "mlp.cu", "trans.cu"]
 
 
 def _nvcc() -> str:

@@ -65,8 +65,11 @@ def test_flag_requires_directory_and_bad_values(driver, tmp_path):
     assert r.returncode != 0 and "Unknown logical value" in r.stderr
     r = run(driver, tmp_path, DiscFlg="true")
     assert r.returncode != 0 and "specify 'beta'" in r.stderr
-    r = run(driver, tmp_path, TransRun="true")
-    assert r.returncode != 0 and "TransRun" in r.stderr
+    # TransICFlg given (true or false) needs TransICDir, also in a transient run.
+    r = run(driver, tmp_path, TransRun="true", TransICFlg="false", TransICDir=None)
+    assert r.returncode != 0 and "Must specify 'TransICDir'" in r.stderr
+    r = run(driver, tmp_path, TransSaveMod="2.5")
+    assert r.returncode != 0 and "no integer value" in r.stderr
 
 
 def test_defaults_are_announced(driver, tmp_path):
@@ -74,6 +77,15 @@ def test_defaults_are_announced(driver, tmp_path):
     out = r.stdout
     assert "Setting 'k' to default value: 3" in out
     assert "Setting 'q' to default value: 0" in out
+    # The transient-run keys default only in a transient run
+    # (SourceCode/ReadUserInput.c:142-171).
+    assert "TransSaveMod" not in out
+    r = run(driver, tmp_path, TransRun="true", TransICDir=None)
+    out = r.stdout
+    for key, val in [("TransICFlg", "0"), ("TransDivVal", "1000"), ("TransConVal", "1e-08"), ("TransSave", "0"),
+                     ("TransRemovalEst", "0"), ("TransSaveMod", "100"), ("TransPeriods", "1")]:
+        assert f"Setting '{key}' to default value: {val}" in out, key
+    assert "Must specify 'TransICDir'" not in r.stderr
 
 
 @pytest.mark.gpu
@@ -115,3 +127,39 @@ def test_end_to_end_matches_the_library(driver, tmp_path, opt):
     r = run(driver, tmp_path, InputForcingFlg="true", InputForcingDir="F", q=0, SaveResultsOpt=opt)
     assert r.returncode == 0
     assert (tmp_path / "ResolventModes_1" / "S_hat").exists()
+
+
+@pytest.mark.gpu
+def test_transient_run_writes_the_reference_files(driver, tmp_path):
+    """TransRun: true from a given initial vector (TransICFlg, path RootDir +
+    ResultsDir + TransICDir): TransientSnapshots_0/ holds q_transient_<pos>
+    every TransSaveMod steps, q_transient_norms, q_transient_last_snapshot,
+    the per-period estimate vectors and the inputs copy
+    (SourceCode/TransientRunRK4.c:116-222), matching the oracle."""
+    from oracle import trans_ref
+    A = synth.gl_operator(64, mu0=0.2)
+    petsc_io.write_mat(str(tmp_path / "A"), A)
+    q0 = synth.complex_normal(64, 1, 21)[:, 0]
+    petsc_io.write_vec(str(tmp_path / "ic"), q0)
+    r = run(driver, tmp_path, TransRun="true", TransICFlg="true", TransICDir="ic", TransSave="true",
+            TransSaveMod=60, TransPeriods=2, TransRemovalEst="true", TransConVal=0)
+    assert r.returncode == 0, r.stderr + r.stdout
+    folder = tmp_path / "TransientSnapshots_0"
+    ref = trans_ref.trans_run(A, q0, 0.1, 8, trans_ref.grid_dt(0.1, 8, 0.15), periods=2, save_mod=60, con_val=0.0,
+                              removal_est_flag=True)
+    norms = petsc_io.read_vec(str(folder / "q_transient_norms"))
+    assert norms.size == ref["norms"].size and np.abs(norms.imag).max() == 0
+    assert (np.abs(norms.real - ref["norms"]) <= 1e-12 * ref["norms"]).all()
+    last = petsc_io.read_vec(str(folder / "q_transient_last_snapshot"))
+    assert np.linalg.norm(last - ref["q"]) <= 1e-12 * np.linalg.norm(ref["q"])
+    for pos, v in ref["snapshots"].items():
+        got = petsc_io.read_vec(str(folder / f"q_transient_{pos}"))
+        assert np.linalg.norm(got - v) <= 1e-12 * np.linalg.norm(v), pos
+    assert not (folder / f"q_transient_{len(ref['snapshots'])}").exists()
+    for p, ini, upd in ref["estimates"]:
+        gi = petsc_io.read_vec(str(folder / f"Initial_transient_norm_period_{p}")).real
+        gu = petsc_io.read_vec(str(folder / f"Updated_transient_norm_period_{p}")).real
+        assert gi.size == 4 and (np.abs(gi - ini) <= 1e-11 * ini).all()
+        assert np.abs(gu - upd).max() < 1e-12
+    assert (folder / "variables.yaml").exists()
+    assert "Transient run" in r.stdout and "Total snapshots to be saved" in r.stdout
