@@ -46,9 +46,14 @@ typedef enum {
 typedef enum { RSVDT_ADJOINT = 0, RSVDT_DIRECT = 1 } rsvdt_dir;
 
 typedef enum {
-  RSVDT_PREC_C128 = 0, /* plain form: complex128 throughout */
-  RSVDT_PREC_C64 = 1   /* precision form: complex64 operator/state/stages, FP32
-                          accumulation; FP64 DFT, QR, SVD and spectral blocks */
+  RSVDT_PREC_C128 = 0,       /* plain form: complex128 throughout */
+  RSVDT_PREC_C64 = 1,        /* precision form: complex64 operator/state/stages, FP32
+                                accumulation; FP64 DFT, QR, SVD and spectral blocks */
+  RSVDT_PREC_C64_REFINE = 2  /* precision form with one FP64 sweep: every action in
+                                complex64 except the last adjoint action of
+                                rsvdt_run, which runs in complex128 (the gains it
+                                yields then carry the complex64 subspace error only
+                                to second order) */
 } rsvdt_precision;
 
 /* Weight / input / output matrices (SourceCode/Variables.h:69-80). */

@@ -373,6 +373,7 @@ rsvdt_status rsvdt_create(const rsvdt_params *p, rsvdt_ctx **out) {
   *out = nullptr;
   rsvdt_ctx *ctx = new rsvdt_ctx();
   ctx->par = *p;
+  ctx->act_prec = base_precision(p->precision);
   rsvdt_status st = RSVDT_OK;
   if (p->k < 1) st = set_err(ctx, RSVDT_ERR_ARG, "'k' must be positive, current value: %lld", (long long)p->k);
   else if (p->q < 0) st = set_err(ctx, RSVDT_ERR_ARG, "'q' must be non-negative, current value: %lld", (long long)p->q);
@@ -382,7 +383,8 @@ rsvdt_status rsvdt_create(const rsvdt_params *p, rsvdt_ctx **out) {
   else if (!(p->TransientLength >= 0)) st = set_err(ctx, RSVDT_ERR_ARG, "Must specify 'TransientLength'");
   else if (p->DiscFlg && p->beta < 0)
     st = set_err(ctx, RSVDT_ERR_ARG, "'beta' must be positive, current value: %g", p->beta);
-  else if (p->precision != RSVDT_PREC_C128 && p->precision != RSVDT_PREC_C64)
+  else if (p->precision != RSVDT_PREC_C128 && p->precision != RSVDT_PREC_C64 &&
+           p->precision != RSVDT_PREC_C64_REFINE)
     st = set_err(ctx, RSVDT_ERR_ARG, "unknown precision %d", (int)p->precision);
   if (st == RSVDT_OK) {
     int ndev = 0;
@@ -657,7 +659,7 @@ rsvdt_status rsvdt_action(rsvdt_ctx *ctx, rsvdt_dir dir) {
   const int d = dir == RSVDT_DIRECT ? 1 : 0;
   int64_t rend = 0;
   RSVDT_TRY(rsvdt::action_prepare(ctx, d, &rend));
-  RSVDT_TRY(run_steps(ctx, d, ctx->par.precision, 1, rend, true));
+  RSVDT_TRY(run_steps(ctx, d, ctx->act_prec, 1, rend, true));
   return rsvdt::action_finish(ctx, d);
 }
 
@@ -668,7 +670,7 @@ namespace rsvdt {
 // First half of an action: weights before, forcing slabs, y = 0 and the
 // initial forcing; returns the number of RK4 steps (SourceCode/TSActionRK4.c:41-42).
 rsvdt_status action_prepare(rsvdt_ctx *ctx, int d, int64_t *rend_out) {
-  const int prec = ctx->par.precision;
+  const int prec = ctx->act_prec;
   RSVDT_TRY(check_weights(ctx));
   const int64_t rows_in = d ? ctx->Nb : ctx->Nc;
   if (ctx->blk_rows != rows_in)
@@ -697,7 +699,7 @@ rsvdt_status action_prepare(rsvdt_ctx *ctx, int d, int64_t *rend_out) {
 
 // Second half: DFT or transient removal, weights after, finiteness check.
 rsvdt_status action_finish(rsvdt_ctx *ctx, int d) {
-  const int prec = ctx->par.precision;
+  const int prec = ctx->act_prec;
   const bool tr = ctx->par.TransientRemoval != 0;
   if (tr) {
     RSVDT_TRY(transient_removal(ctx, d, prec, ctx->blk2));
@@ -787,7 +789,12 @@ rsvdt_status rsvdt_run(rsvdt_ctx *ctx) {
   RSVDT_TRY(rsvdt_action(ctx, RSVDT_DIRECT));      // SourceCode/main.c:134
   RSVDT_TRY(rsvdt_power_iteration(ctx));           // :136
   RSVDT_TRY(rsvdt_svd_all_freqs(ctx, 1));          // :138-140
-  RSVDT_TRY(rsvdt_action(ctx, RSVDT_ADJOINT));     // :142
+  // The refinement form's FP64 sweep: the last adjoint action, whose
+  // output gives the gains, in complex128.
+  if (ctx->par.precision == RSVDT_PREC_C64_REFINE) ctx->act_prec = RSVDT_PREC_C128;
+  const rsvdt_status st = rsvdt_action(ctx, RSVDT_ADJOINT);  // :142
+  ctx->act_prec = base_precision(ctx->par.precision);
+  RSVDT_TRY(st);
   RSVDT_TRY(rsvdt_svd_all_freqs(ctx, 0));          // :144
   return RSVDT_OK;
 }
@@ -819,7 +826,7 @@ rsvdt_status rsvdt_get_results(rsvdt_ctx *ctx, double *U, int64_t ldu, double *V
 rsvdt_status rsvdt_rk4_reset(rsvdt_ctx *ctx, rsvdt_dir dir) {
   RSVDT_TRY(require_ready(ctx, true));
   if (ctx->blk_rows != ctx->N) return set_err(ctx, RSVDT_ERR_STATE, "working block must have N rows");
-  const int prec = ctx->par.precision;
+  const int prec = ctx->act_prec;
   ctx->Nstore = ctx->par.TransientRemoval ? ctx->Nw + 1 : ctx->Nw;
   RSVDT_TRY(stage_forcing(ctx, prec));
   RSVDT_TRY(launch_forcing_init(ctx, dir == RSVDT_DIRECT ? 1 : 0, prec));
@@ -829,20 +836,20 @@ rsvdt_status rsvdt_rk4_reset(rsvdt_ctx *ctx, rsvdt_dir dir) {
 rsvdt_status rsvdt_rk4_advance(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps) {
   RSVDT_TRY(require_ready(ctx, true));
   if (i0 < 1 || nsteps < 0) return set_err(ctx, RSVDT_ERR_ARG, "invalid step range");
-  return run_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, ctx->par.precision, i0, nsteps, true);
+  return run_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, ctx->act_prec, i0, nsteps, true);
 }
 
 rsvdt_status rsvdt_rk4_profile(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps, double *stage_ms) {
   RSVDT_TRY(require_ready(ctx, true));
   if (i0 < 1 || nsteps < 1 || !stage_ms) return set_err(ctx, RSVDT_ERR_ARG, "invalid profile arguments");
-  return profile_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, ctx->par.precision, i0, nsteps, stage_ms);
+  return profile_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, ctx->act_prec, i0, nsteps, stage_ms);
 }
 
 rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps, double *y, double *F3) {
   RSVDT_TRY(require_ready(ctx, true));
   if (!y || !F3) return set_err(ctx, RSVDT_ERR_ARG, "null state");
   if (ctx->blk_rows != ctx->N) return set_err(ctx, RSVDT_ERR_STATE, "working block must have N rows");
-  const int prec = ctx->par.precision;
+  const int prec = ctx->act_prec;
   const int64_t N = ctx->N, K = ctx->K;
   ctx->Nstore = ctx->par.TransientRemoval ? ctx->Nw + 1 : ctx->Nw;
   RSVDT_TRY(stage_forcing(ctx, prec));

@@ -161,14 +161,23 @@ struct rsvdt_ctx {
   void *scratch = nullptr;
   size_t scratch_bytes = 0;
 
-  // Cached CUDA graphs of G RK4 steps per direction.
+  // Precision of the running action (rsvdt_precision's C128 or C64).
+  int act_prec = 0;
+  // Cached CUDA graphs of G RK4 steps per direction, and their precision.
   cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
+  int step_graph_prec[2] = {-1, -1};
   int64_t step_graph_len = 0;
 
   std::vector<void *> allocations;
 };
 
 namespace rsvdt {
+
+// Stage precision of an action under a params precision: complex128 for the
+// plain form, complex64 for both precision forms.
+inline int base_precision(int precision) {
+  return precision == RSVDT_PREC_C128 ? RSVDT_PREC_C128 : RSVDT_PREC_C64;
+}
 
 // Returns false and records the message when a CUDA call failed.
 bool cuda_ok(rsvdt_ctx *ctx, cudaError_t e, const char *what);

@@ -845,7 +845,14 @@ static rsvdt_status run_steps_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t nst
   int64_t full = nsteps / kGraphSteps, rest = nsteps % kGraphSteps;
   if (full > 0) {
     cudaGraphExec_t &ge = ctx->step_graph[dir ? 1 : 0];
+    int &gprec = ctx->step_graph_prec[dir ? 1 : 0];
+    const int prec = sizeof(Z) == sizeof(z64) ? RSVDT_PREC_C64 : RSVDT_PREC_C128;
+    if (ge && gprec != prec) {
+      cudaGraphExecDestroy(ge);
+      ge = nullptr;
+    }
     if (!ge) {
+      gprec = prec;
       cudaGraph_t g;
       if (!cuda_ok(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal),
                    "begin capture"))

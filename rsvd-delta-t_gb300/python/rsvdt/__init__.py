@@ -24,7 +24,7 @@ LIB_PATH = _build.LIB_PATH
 
 OK, ERR_ARG, ERR_IO, ERR_OOM, ERR_CUDA, ERR_NOT_SPD, ERR_DIVERGED, ERR_TIMEOUT, ERR_STATE = range(9)
 ADJOINT, DIRECT = 0, 1
-PREC_C128, PREC_C64 = 0, 1
+PREC_C128, PREC_C64, PREC_C64_REFINE = 0, 1, 2
 W_F_SQRT_INV, B, C_OUT, W_Q_SQRT, W_Q_SQRT_INV = range(5)
 
 STATUS_NAMES = {0: "OK", 1: "ARG", 2: "IO", 3: "OOM", 4: "CUDA", 5: "NOT_SPD", 6: "DIVERGED",

@@ -61,12 +61,12 @@ class Workload:
         S_v = N k s_c (one state-sized vector pass), 19 vector passes
         (stage inputs formed from y and the previous stage, forcing written
         once and read by the stages that add it), one ring sample every R
-        steps. Stage 1 alone: S_A + S_F + 5 S_v."""
+        steps. Stage 1 alone: S_A + S_F + 5 S_v; stage 2 (or 3): S_A + 4 S_v."""
         S_A = self.operator_bytes(s_c)
         S_F = self.N * self.Nw * self.k * s_c
         S_v = self.N * self.k * s_c
         return dict(S_A=S_A, S_F=S_F, S_v=S_v, step=4 * S_A + S_F + 19 * S_v + S_v / R,
-                    stage1=S_A + S_F + 5 * S_v)
+                    stage1=S_A + S_F + 5 * S_v, stage234=S_A + 4 * S_v)
 
     def step_flops(self, paired: bool = True) -> dict:
         """Arithmetic of one step as executed: 8 flops per complex

@@ -273,6 +273,35 @@ def test_c64_form_close_to_c128(built_lib):
     g64.close()
 
 
+def test_refine_form_recovers_fp64_gains(built_lib):
+    """Precision form with one FP64 sweep (the last adjoint action in
+    complex128): on the non-normal Ginzburg-Landau operator its gains are
+    closer to the complex128 plain form than the all-complex64 form's for
+    the leading mode."""
+    import rsvdt
+    A, cfg = small_gl()
+    k = 4
+    F = None
+    S = {}
+    for prec in (rsvdt.PREC_C128, rsvdt.PREC_C64, rsvdt.PREC_C64_REFINE):
+        ctx = make_ctx(A, cfg, k=k, q=1, tr=True, prec=prec)
+        if F is None:
+            F = synth.complex_normal(A.shape[0], k * ctx.grid().Nw_eff, 15)
+        ctx.set_sketch(F)
+        ctx.run()
+        S[prec] = ctx.get_results()[2]
+        # The context keeps its precision form across runs.
+        ctx.set_sketch(F)
+        ctx.run()
+        assert np.array_equal(ctx.get_results()[2], S[prec])
+        ctx.close()
+    e64 = (np.abs(S[rsvdt.PREC_C64] - S[rsvdt.PREC_C128]) / S[rsvdt.PREC_C128])
+    eref = (np.abs(S[rsvdt.PREC_C64_REFINE] - S[rsvdt.PREC_C128]) / S[rsvdt.PREC_C128])
+    print("refine vs c64 gain errors, mode 1:", eref[0].max(), e64[0].max(), "modes<=3:", eref[:3].max(),
+          e64[:3].max())
+    assert eref[0].max() < e64[0].max() and eref[:3].max() < 1e-3
+
+
 def test_diverged_and_state_errors(built_lib):
     import rsvdt
     A, cfg = small_gl()
