@@ -198,6 +198,29 @@ rsvdt_status rsvdt_rk4_advance(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_
 rsvdt_status rsvdt_rk4_profile(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps,
                                double *stage_ms);
 
+/* ----------------------------------------------------------- capacity mode
+ * For problems whose spectral blocks do not fit several times in device
+ * memory (N = 10.5M, k = 16, Nw = 64: one block is 172 GB in complex128):
+ * every action runs its test vectors in chunks of kc (kc divides k; 0 picks
+ * the largest chunk that fits) and writes each chunk's response into its own
+ * columns of the one working block; the weight products and the SVDs work in
+ * place; U is kept in host memory (complex64 when u_c64 is set) from the SVD
+ * before the adjoint to the end. Results equal the resident mode's to
+ * rounding. Call before the sketch (best right after rsvdt_create, so that
+ * the resident buffers are never allocated); set the weights before the
+ * sketch too. rsvdt_rk4_steps is not available in this mode. */
+rsvdt_status rsvdt_set_capacity_mode(rsvdt_ctx *ctx, int64_t kc, int32_t u_c64);
+/* Chunk size in use (0 when the context is not in capacity mode). */
+rsvdt_status rsvdt_get_capacity(const rsvdt_ctx *ctx, int64_t *kc);
+
+/* Columns cols[0..ncols) (indices iw*k + ik) of U (Nc rows) and V (Nb rows)
+ * after rsvdt_run, column-major with leading dimensions ldu / ldv; U or V
+ * may be NULL. For results too large to fetch whole (e.g. the files of
+ * SourceCode/SaveResults.c:46-85, one test vector or one frequency at a
+ * time). */
+rsvdt_status rsvdt_get_result_cols(rsvdt_ctx *ctx, const int64_t *cols, int64_t ncols, double *U, int64_t ldu,
+                                   double *V, int64_t ldv);
+
 /* ------------------------------------------------------ transient simulation
  * The initial-value problem dq/dt = A q (A discounted when DiscFlg) by
  * unforced RK4 from a given initial vector, with the norm checked every

@@ -6,6 +6,8 @@
 #include <cstring>
 #include <vector>
 
+#include <unistd.h>
+
 #include "common.cuh"
 
 using namespace rsvdt;
@@ -247,38 +249,103 @@ static rsvdt_status setup_grid_and_tables(rsvdt_ctx *ctx) {
 }
 
 // Device buffers for K test vectors.
+// Complex values of each of the capacity mode's two chunk buffers (the
+// ring and the forcing slabs, which double as temporaries of the chunked
+// weight products) for a chunk of Ks test vectors.
+static size_t cap_chunk_elems(const rsvdt_ctx *ctx, int64_t Ks, int64_t rows) {
+  const int64_t Nstore = ctx->Nw + 1;
+  return (size_t)std::max(Nstore * ctx->N, rows * ctx->Nw_eff) * Ks;
+}
+
+// Largest chunk (a divisor of K) whose buffers fit in the free device
+// memory, counting the working block if it is not allocated yet and the
+// transient-removal buffers.
+static int64_t cap_choose_chunk(rsvdt_ctx *ctx, int64_t K, int64_t rows) {
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  // Buffers this context would free before allocating new ones.
+  size_t held = 0;
+  if (ctx->y) held += sizeof(z128) * 6 * (size_t)ctx->N * ctx->Ks;
+  if (ctx->ring) held += sizeof(z128) * 2 * cap_chunk_elems(ctx, ctx->Ks, rows);
+  size_t avail = fr + held;
+  const size_t blk = sizeof(z128) * (size_t)rows * ctx->Nw_eff * K;
+  if (!ctx->blk || ctx->blk_elems < (size_t)rows * ctx->Nw_eff * K) avail = avail > blk ? avail - blk : 0;
+  const size_t tr = ctx->par.TransientRemoval
+                        ? sizeof(z128) * (2 * (size_t)ctx->N * (ctx->Nw + 1) + 2 * (size_t)ctx->N * ctx->Nw_eff)
+                        : 0;
+  // Gram partials of the CholQR passes (chunks of 2048 rows x nw x K^2).
+  const size_t gram = sizeof(z128) * (size_t)((rows + 2047) / 2048 + 8) * ctx->Nw_eff * K * K;
+  const size_t margin = ((size_t)2 << 30) + tr + gram;
+  for (int64_t kc = K; kc >= 1; --kc) {
+    if (K % kc) continue;
+    const size_t need = sizeof(z128) * (6 * (size_t)ctx->N * kc + 2 * cap_chunk_elems(ctx, kc, rows)) + margin;
+    if (need <= avail) return kc;
+  }
+  return 1;
+}
+
 static rsvdt_status ensure_buffers(rsvdt_ctx *ctx, int64_t K) {
   const int64_t N = ctx->N, Nwe = ctx->Nw_eff;
   const int64_t rows = std::max(N, std::max(ctx->Nb, ctx->Nc));
   const size_t blk_elems = (size_t)rows * Nwe * K;
   const int64_t Nstore = ctx->Nw + 1;  // room for the transient-removal sample
-  if (ctx->K == K && ctx->y && ctx->blk_elems >= blk_elems) return RSVDT_OK;
+  int64_t Ks = K;
+  if (ctx->capacity) {
+    Ks = ctx->cap_kc > 0 ? ctx->cap_kc : cap_choose_chunk(ctx, K, rows);
+    if (K % Ks != 0)
+      return set_err(ctx, RSVDT_ERR_ARG, "capacity chunk %lld does not divide k = %lld", (long long)Ks, (long long)K);
+  }
+  if (ctx->K == K && ctx->Ks == Ks && ctx->y && ctx->blk_elems >= blk_elems && ctx->buf_capacity == ctx->capacity)
+    return RSVDT_OK;
   free_graphs(ctx);
   void **bufs[] = {&ctx->y, &ctx->zA, &ctx->zB, &ctx->acc, &ctx->F2, &ctx->F3};
   for (auto b : bufs) {
     dfree(ctx, *b);
-    *b = dalloc(ctx, sizeof(z128) * N * K);
+    *b = dalloc(ctx, sizeof(z128) * N * Ks);
     if (!*b) return set_err(ctx, RSVDT_ERR_OOM, "state allocation failed");
   }
   dfree(ctx, ctx->ring);
-  ctx->ring = dalloc(ctx, sizeof(z128) * Nstore * N * K);
   dfree(ctx, ctx->Fh);
-  ctx->Fh = dalloc(ctx, sizeof(z128) * N * Nwe * K);
-  // Keep the working block's contents when it is only re-sized upward.
-  z128 *old = ctx->blk;
-  size_t old_elems = ctx->blk_elems;
-  z128 *nb = (z128 *)dalloc(ctx, sizeof(z128) * blk_elems);
-  if (nb && old) cudaMemcpy(nb, old, sizeof(z128) * std::min(old_elems, blk_elems), cudaMemcpyDeviceToDevice);
-  dfree(ctx, old);
-  ctx->blk = nb;
   dfree(ctx, ctx->blk2);
-  ctx->blk2 = (z128 *)dalloc(ctx, sizeof(z128) * blk_elems);
+  ctx->blk2 = nullptr;
+  if (ctx->capacity) {
+    const size_t ce = cap_chunk_elems(ctx, Ks, rows);
+    ctx->ring = dalloc(ctx, sizeof(z128) * ce);
+    ctx->Fh = dalloc(ctx, sizeof(z128) * ce);
+  } else {
+    ctx->ring = dalloc(ctx, sizeof(z128) * Nstore * N * K);
+    ctx->Fh = dalloc(ctx, sizeof(z128) * N * Nwe * K);
+  }
+  if (ctx->capacity) {
+    // One working block, re-allocated only when it must grow (its contents
+    // are then lost: set the weights before the sketch).
+    if (!ctx->blk || ctx->blk_elems < blk_elems) {
+      dfree(ctx, ctx->blk);
+      ctx->blk = (z128 *)dalloc(ctx, sizeof(z128) * blk_elems);
+      ctx->blk_elems = ctx->blk ? blk_elems : 0;
+    }
+  } else {
+    // Keep the working block's contents when it is only re-sized upward.
+    z128 *old = ctx->blk;
+    size_t old_elems = ctx->blk_elems;
+    z128 *nb = (z128 *)dalloc(ctx, sizeof(z128) * blk_elems);
+    if (nb && old) cudaMemcpy(nb, old, sizeof(z128) * std::min(old_elems, blk_elems), cudaMemcpyDeviceToDevice);
+    dfree(ctx, old);
+    ctx->blk = nb;
+    ctx->blk2 = (z128 *)dalloc(ctx, sizeof(z128) * blk_elems);
+    ctx->blk_elems = blk_elems;
+  }
   dfree(ctx, ctx->S);
   ctx->S = (double *)dalloc(ctx, sizeof(double) * Nwe * K);
-  if (!ctx->ring || !ctx->Fh || !ctx->blk || !ctx->blk2 || !ctx->S)
+  if (!ctx->ring || !ctx->Fh || !ctx->blk || (!ctx->capacity && !ctx->blk2) || !ctx->S)
     return set_err(ctx, RSVDT_ERR_OOM, "spectral block allocation failed (%zu complex values each)", blk_elems);
-  ctx->blk_elems = blk_elems;
   ctx->K = K;
+  ctx->Ks = Ks;
+  ctx->k0 = 0;
+  ctx->buf_capacity = ctx->capacity;
   return RSVDT_OK;
 }
 
@@ -324,14 +391,27 @@ static rsvdt_status check_weights(rsvdt_ctx *ctx) {
     if (_s != RSVDT_OK) return _s;     \
   } while (0)
 
-// Y <- M Y on the working block (ping-pong between blk and blk2).
+// Y <- M Y on the working block: ping-pong between blk and blk2, or in
+// capacity mode chunk by chunk through the forcing-slab and ring buffers
+// (each chunk is its own columns of the block, so chunks never overlap,
+// whatever the row counts).
 static rsvdt_status weight_step(rsvdt_ctx *ctx, const DevCSR &M, int64_t rows_in) {
   if (!M.present) return RSVDT_OK;
   if (M.cols != rows_in)
     return set_err(ctx, RSVDT_ERR_ARG, "weight product: %lld columns but the block has %lld rows",
                    (long long)M.cols, (long long)rows_in);
-  RSVDT_TRY(apply_weight(ctx, M, ctx->blk, ctx->blk2, ctx->Nw_eff * ctx->K));
-  std::swap(ctx->blk, ctx->blk2);
+  if (ctx->capacity) {
+    const int64_t K = ctx->K, Ks = ctx->Ks, Nwe = ctx->Nw_eff;
+    z128 *tA = (z128 *)ctx->Fh, *tB = (z128 *)ctx->ring;
+    for (int64_t k0 = 0; k0 < K; k0 += Ks) {
+      RSVDT_TRY(launch_chunk_copy(ctx, ctx->blk, tA, rows_in, Nwe, K, k0, Ks, true));
+      RSVDT_TRY(apply_weight(ctx, M, tA, tB, Nwe * Ks));
+      RSVDT_TRY(launch_chunk_copy(ctx, tB, ctx->blk, M.rows, Nwe, K, k0, Ks, false));
+    }
+  } else {
+    RSVDT_TRY(apply_weight(ctx, M, ctx->blk, ctx->blk2, ctx->Nw_eff * ctx->K));
+    std::swap(ctx->blk, ctx->blk2);
+  }
   ctx->blk_rows = M.rows;
   return RSVDT_OK;
 }
@@ -340,6 +420,138 @@ static rsvdt_status weight_step(rsvdt_ctx *ctx, const DevCSR &M, int64_t rows_in
 // action's precision (TSActionRK4 copies Y_hat to F_hat,
 // SourceCode/TSActionRK4.c:49).
 static rsvdt_status stage_forcing(rsvdt_ctx *ctx, int prec) { return stage_forcing_coeffs(ctx, prec); }
+
+namespace rsvdt {
+static rsvdt_status cap_action(rsvdt_ctx *ctx, int d);
+}
+
+// ---------------------------------------------------------- capacity mode
+
+// Free host memory in bytes (what can be allocated without swapping).
+static size_t host_avail_bytes() {
+  const long pages = sysconf(_SC_AVPHYS_PAGES), psz = sysconf(_SC_PAGESIZE);
+  return pages > 0 && psz > 0 ? (size_t)pages * (size_t)psz : 0;
+}
+
+// StoreU in capacity mode (SourceCode/StoreU.c:15): U goes to host memory
+// chunk by chunk, already multiplied by W_q^{-1/2} (SourceCode/SVDAllFreqs.c:63
+// applies it at the end; U does not change in between), in complex128 or
+// complex64, layout [row][iw][kc] per chunk.
+static rsvdt_status cap_store_u(rsvdt_ctx *ctx, int64_t rows) {
+  const int64_t K = ctx->K, Ks = ctx->Ks, Nwe = ctx->Nw_eff;
+  const DevCSR &Wi = ctx->W[RSVDT_W_Q_SQRT_INV];
+  if (Wi.present && Wi.cols != rows)
+    return set_err(ctx, RSVDT_ERR_ARG, "W_q^{-1/2} has %lld columns, U has %lld rows", (long long)Wi.cols,
+                   (long long)rows);
+  const int64_t urows = Wi.present ? Wi.rows : rows;
+  const size_t es = ctx->cap_u_c64 ? sizeof(z64) : sizeof(z128);
+  const size_t cbytes = es * (size_t)urows * Nwe * Ks;
+  const int64_t nch = K / Ks;
+  ctx->u_host.clear();
+  const size_t need = cbytes * (size_t)nch, margin = (size_t)8 << 30;
+  if (need + margin > host_avail_bytes())
+    return set_err(ctx, RSVDT_ERR_OOM,
+                   "U needs %.1f GB of host memory and %.1f GB are free (complex64 storage halves it)",
+                   need / 1e9, host_avail_bytes() / 1e9);
+  z128 *tA = (z128 *)ctx->Fh, *tB = (z128 *)ctx->ring;
+  for (int64_t c = 0; c < nch; ++c) {
+    std::vector<unsigned char> h;
+    try {
+      h.resize(cbytes);
+    } catch (...) {
+      ctx->u_host.clear();
+      return set_err(ctx, RSVDT_ERR_OOM, "host allocation of %zu bytes for U failed", cbytes);
+    }
+    RSVDT_TRY(launch_chunk_copy(ctx, ctx->blk, tA, rows, Nwe, K, c * Ks, Ks, true));
+    const z128 *src = tA;
+    if (Wi.present) {
+      RSVDT_TRY(apply_weight(ctx, Wi, tA, tB, Nwe * Ks));
+      src = tB;
+    }
+    const void *dsrc = src;
+    if (ctx->cap_u_c64) {
+      z64 *d64 = (z64 *)(src == tA ? tB : tA);
+      RSVDT_TRY(launch_convert_to64(ctx, src, d64, urows * Nwe * Ks));
+      dsrc = d64;
+    }
+    if (!cuda_ok(ctx, cudaMemcpyAsync(h.data(), dsrc, cbytes, cudaMemcpyDeviceToHost, ctx->stream), "U download") ||
+        !cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync"))
+      return RSVDT_ERR_CUDA;
+    ctx->u_host.push_back(std::move(h));
+  }
+  ctx->U_rows = urows;
+  return RSVDT_OK;
+}
+
+// SVDAllFreqsBeforeAdjoint + StoreU, or SVDAllFreqs, in capacity mode: the
+// SVD is in place (the block becomes U, or V), U goes to the host, and
+// V <- W_f^{-1/2} V is applied chunk by chunk in the block.
+static rsvdt_status cap_svd(rsvdt_ctx *ctx, bool before_adjoint) {
+  const int64_t rows = ctx->blk_rows;
+  if (!before_adjoint && ctx->u_host.empty())
+    return set_err(ctx, RSVDT_ERR_STATE, "U has not been stored (run the SVD before the adjoint first)");
+  RSVDT_TRY(svd_all(ctx, ctx->blk, rows, ctx->Nw_eff, ctx->K, nullptr, ctx->S));
+  if (before_adjoint) {
+    RSVDT_TRY(cap_store_u(ctx, rows));
+  } else {
+    RSVDT_TRY(weight_step(ctx, ctx->W[RSVDT_W_F_SQRT_INV], rows));
+    ctx->have_results = true;
+  }
+  return cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
+}
+
+// Columns cols[0..ncols) (indices iw*K + k; all C columns when cols is
+// null) of a device block [row][iw][k] (rows x C) into a column-major host
+// array, through row batches of about 64 MB.
+static rsvdt_status block_cols_to_host(rsvdt_ctx *ctx, const z128 *src, int64_t rows, int64_t C, const int64_t *cols,
+                                       int64_t ncols, double *out, int64_t ld) {
+  const int64_t batch = std::max<int64_t>(1, ((int64_t)64 << 20) / (int64_t)(sizeof(z128) * C));
+  std::vector<z128> tmp((size_t)std::min(rows, batch) * C);
+  for (int64_t r0 = 0; r0 < rows; r0 += batch) {
+    const int64_t nr = std::min(batch, rows - r0);
+    if (!cuda_ok(ctx, cudaMemcpyAsync(tmp.data(), src + r0 * C, sizeof(z128) * nr * C, cudaMemcpyDeviceToHost,
+                                      ctx->stream),
+                 "download") ||
+        !cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync"))
+      return RSVDT_ERR_CUDA;
+    for (int64_t j = 0; j < ncols; ++j) {
+      const int64_t c = cols ? cols[j] : j;
+      double *o = out + 2 * (j * ld + r0);
+      for (int64_t r = 0; r < nr; ++r) {
+        const z128 v = tmp[(size_t)(r * C + c)];
+        o[2 * r] = v.re;
+        o[2 * r + 1] = v.im;
+      }
+    }
+  }
+  return RSVDT_OK;
+}
+
+// The same from the host copy of U (capacity mode).
+static void host_u_cols(const rsvdt_ctx *ctx, const int64_t *cols, int64_t ncols, double *out, int64_t ld) {
+  const int64_t K = ctx->K, Ks = ctx->Ks, Nwe = ctx->Nw_eff, rows = ctx->U_rows;
+  for (int64_t j = 0; j < ncols; ++j) {
+    const int64_t col = cols ? cols[j] : j;
+    const int64_t iw = col / K, k = col % K, c = k / Ks, kc = k % Ks;
+    double *o = out + 2 * j * ld;
+    if (ctx->cap_u_c64) {
+      const z64 *h = (const z64 *)ctx->u_host[(size_t)c].data();
+      for (int64_t r = 0; r < rows; ++r) {
+        const z64 v = h[(size_t)((r * Nwe + iw) * Ks + kc)];
+        o[2 * r] = v.re;
+        o[2 * r + 1] = v.im;
+      }
+    } else {
+      const z128 *h = (const z128 *)ctx->u_host[(size_t)c].data();
+      for (int64_t r = 0; r < rows; ++r) {
+        const z128 v = h[(size_t)((r * Nwe + iw) * Ks + kc)];
+        o[2 * r] = v.re;
+        o[2 * r + 1] = v.im;
+      }
+    }
+  }
+}
+
 
 static rsvdt_status require_ready(rsvdt_ctx *ctx, bool need_block) {
   if (!ctx) return RSVDT_ERR_ARG;
@@ -613,6 +825,27 @@ rsvdt_status rsvdt_set_sketch(rsvdt_ctx *ctx, const double *F, int64_t ld, int64
                    (long long)ctx->Nw_eff, (long long)ctx->Nb, (long long)ncols);
   RSVDT_TRY(ensure_buffers(ctx, ncols / ctx->Nw_eff));
   const int64_t K = ctx->K, C = ctx->Nw_eff * K, rows = ctx->Nb;
+  if (ctx->capacity) {
+    // Row batches transposed on the host (no block-sized staging buffer).
+    const int64_t batch = std::max<int64_t>(1, ((int64_t)64 << 20) / (int64_t)(sizeof(z128) * C));
+    std::vector<z128> tmp((size_t)std::min(rows, batch) * C);
+    for (int64_t r0 = 0; r0 < rows; r0 += batch) {
+      const int64_t nr = std::min(batch, rows - r0);
+      for (int64_t c = 0; c < C; ++c) {
+        const double *f = F + 2 * (c * ld + r0);
+        for (int64_t r = 0; r < nr; ++r) tmp[(size_t)(r * C + c)] = zmake<z128>(f[2 * r], f[2 * r + 1]);
+      }
+      if (!cuda_ok(ctx, cudaMemcpyAsync(ctx->blk + r0 * C, tmp.data(), sizeof(z128) * nr * C, cudaMemcpyHostToDevice,
+                                        ctx->stream),
+                   "upload") ||
+          !cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync"))
+        return RSVDT_ERR_CUDA;
+    }
+    ctx->blk_rows = rows;
+    ctx->have_block = true;
+    ctx->have_results = false;
+    return RSVDT_OK;
+  }
   z128 *stage = (z128 *)dalloc(ctx, sizeof(z128) * ld * C);
   if (!stage) return set_err(ctx, RSVDT_ERR_OOM, "staging allocation failed");
   rsvdt_status st = RSVDT_OK;
@@ -643,6 +876,7 @@ rsvdt_status rsvdt_get_block(rsvdt_ctx *ctx, double *Y, int64_t ld, int64_t *row
   if (rows) *rows = r;
   if (!Y) return RSVDT_OK;
   if (ld < r) return set_err(ctx, RSVDT_ERR_ARG, "ld (%lld) < rows (%lld)", (long long)ld, (long long)r);
+  if (ctx->capacity) return block_cols_to_host(ctx, ctx->blk, r, C, nullptr, C, Y, ld);
   z128 *stage = (z128 *)dalloc(ctx, sizeof(z128) * ld * C);
   if (!stage) return set_err(ctx, RSVDT_ERR_OOM, "staging allocation failed");
   rsvdt_status st = launch_blk_to_colmajor(ctx, ctx->blk, r, C, stage, ld);
@@ -657,6 +891,7 @@ rsvdt_status rsvdt_get_block(rsvdt_ctx *ctx, double *Y, int64_t ld, int64_t *row
 rsvdt_status rsvdt_action(rsvdt_ctx *ctx, rsvdt_dir dir) {
   RSVDT_TRY(require_ready(ctx, true));
   const int d = dir == RSVDT_DIRECT ? 1 : 0;
+  if (ctx->capacity) return cap_action(ctx, d);
   int64_t rend = 0;
   RSVDT_TRY(rsvdt::action_prepare(ctx, d, &rend));
   RSVDT_TRY(run_steps(ctx, d, ctx->act_prec, 1, rend, true));
@@ -669,15 +904,16 @@ namespace rsvdt {
 
 // First half of an action: weights before, forcing slabs, y = 0 and the
 // initial forcing; returns the number of RK4 steps (SourceCode/TSActionRK4.c:41-42).
-rsvdt_status action_prepare(rsvdt_ctx *ctx, int d, int64_t *rend_out) {
-  const int prec = ctx->act_prec;
+// Checks and ApplyWeightMats before the stepping
+// (SourceCode/ApplyWeightMats.c:17-28, 43-60); returns the number of RK4
+// steps of the action (SourceCode/TSActionRK4.c:41-42).
+static rsvdt_status weights_before(rsvdt_ctx *ctx, int d, int64_t *rend_out) {
   RSVDT_TRY(check_weights(ctx));
   const int64_t rows_in = d ? ctx->Nb : ctx->Nc;
   if (ctx->blk_rows != rows_in)
     return set_err(ctx, RSVDT_ERR_STATE, "%s action needs a block of %lld rows, the working block has %lld",
                    d ? "direct" : "adjoint", (long long)rows_in, (long long)ctx->blk_rows);
   if (ctx->par.Display >= 1) printf("\n*** %s action begins! ***\n", d ? "Direct" : "Adjoint");
-  // ApplyWeightMats before (SourceCode/ApplyWeightMats.c:17-28, 43-60).
   if (d) {
     RSVDT_TRY(weight_step(ctx, ctx->W[RSVDT_W_F_SQRT_INV], ctx->blk_rows));
     RSVDT_TRY(weight_step(ctx, ctx->W[RSVDT_B], ctx->blk_rows));
@@ -686,29 +922,16 @@ rsvdt_status action_prepare(rsvdt_ctx *ctx, int d, int64_t *rend_out) {
     RSVDT_TRY(weight_step(ctx, ctx->WH[RSVDT_C], ctx->blk_rows));
   }
   if (ctx->blk_rows != ctx->N) return set_err(ctx, RSVDT_ERR_ARG, "forcing block has %lld rows, expected N", (long long)ctx->blk_rows);
-  // TSActionRK4 (SourceCode/TSActionRK4.c:38-148).
   const bool tr = ctx->par.TransientRemoval != 0;
   ctx->Nstore = tr ? ctx->Nw + 1 : ctx->Nw;
-  const int64_t rend = ctx->Nt + ctx->Ns + (tr ? ctx->R : 0);
-  RSVDT_TRY(stage_forcing(ctx, prec));
+  *rend_out = ctx->Nt + ctx->Ns + (tr ? ctx->R : 0);
   if (!cuda_ok(ctx, cudaMemsetAsync(ctx->d_flags, 0, sizeof(int32_t) * 4, ctx->stream), "memset")) return RSVDT_ERR_CUDA;
-  RSVDT_TRY(launch_forcing_init(ctx, d, prec));
-  *rend_out = rend;
   return RSVDT_OK;
 }
 
-// Second half: DFT or transient removal, weights after, finiteness check.
-rsvdt_status action_finish(rsvdt_ctx *ctx, int d) {
-  const int prec = ctx->act_prec;
-  const bool tr = ctx->par.TransientRemoval != 0;
-  if (tr) {
-    RSVDT_TRY(transient_removal(ctx, d, prec, ctx->blk2));
-  } else {
-    RSVDT_TRY(launch_dft(ctx, prec, ctx->blk2));
-  }
-  std::swap(ctx->blk, ctx->blk2);
-  ctx->blk_rows = ctx->N;
-  // ApplyWeightMats after (SourceCode/ApplyWeightMats.c:29-41, 61-79).
+// ApplyWeightMats after the stepping (SourceCode/ApplyWeightMats.c:29-41,
+// 61-79) and the finiteness check of the response.
+static rsvdt_status weights_after(rsvdt_ctx *ctx, int d) {
   if (d) {
     RSVDT_TRY(weight_step(ctx, ctx->W[RSVDT_C], ctx->blk_rows));
     RSVDT_TRY(weight_step(ctx, ctx->W[RSVDT_W_Q_SQRT], ctx->blk_rows));
@@ -721,6 +944,48 @@ rsvdt_status action_finish(rsvdt_ctx *ctx, int d) {
   if (!ok) return set_err(ctx, RSVDT_ERR_DIVERGED, "NaN or Inf in the %s action's response", d ? "direct" : "adjoint");
   if (ctx->par.Display >= 1) printf("*** %s action done ***\n", d ? "Direct" : "Adjoint");
   return RSVDT_OK;
+}
+
+// First half of an action: weights before, forcing slabs, y = 0 and the
+// initial forcing (TSActionRK4, SourceCode/TSActionRK4.c:38-148).
+rsvdt_status action_prepare(rsvdt_ctx *ctx, int d, int64_t *rend_out) {
+  RSVDT_TRY(weights_before(ctx, d, rend_out));
+  RSVDT_TRY(stage_forcing(ctx, ctx->act_prec));
+  return launch_forcing_init(ctx, d, ctx->act_prec);
+}
+
+// Second half: DFT or transient removal, weights after, finiteness check.
+rsvdt_status action_finish(rsvdt_ctx *ctx, int d) {
+  const int prec = ctx->act_prec;
+  if (ctx->par.TransientRemoval) {
+    RSVDT_TRY(transient_removal(ctx, d, prec, ctx->blk2));
+  } else {
+    RSVDT_TRY(launch_dft(ctx, prec, ctx->blk2));
+  }
+  std::swap(ctx->blk, ctx->blk2);
+  ctx->blk_rows = ctx->N;
+  return weights_after(ctx, d);
+}
+
+// An action in capacity mode: the test vectors go through the stepping in
+// chunks of Ks, each chunk's forcing staged from and its response written
+// back into its own columns of the one working block.
+static rsvdt_status cap_action(rsvdt_ctx *ctx, int d) {
+  const int prec = ctx->act_prec;
+  int64_t rend = 0;
+  RSVDT_TRY(weights_before(ctx, d, &rend));
+  rsvdt_status st = RSVDT_OK;
+  for (int64_t k0 = 0; k0 < ctx->K && !st; k0 += ctx->Ks) {
+    ctx->k0 = k0;
+    st = stage_forcing(ctx, prec);
+    if (!st) st = launch_forcing_init(ctx, d, prec);
+    if (!st) st = run_steps(ctx, d, prec, 1, rend, true);
+    if (!st) st = ctx->par.TransientRemoval ? transient_removal(ctx, d, prec, ctx->blk) : launch_dft(ctx, prec, ctx->blk);
+  }
+  ctx->k0 = 0;
+  RSVDT_TRY(st);
+  ctx->blk_rows = ctx->N;
+  return weights_after(ctx, d);
 }
 
 }  // namespace rsvdt
@@ -736,6 +1001,7 @@ rsvdt_status rsvdt_qr_all_freqs(rsvdt_ctx *ctx) {
 rsvdt_status rsvdt_svd_all_freqs(rsvdt_ctx *ctx, int32_t before_adjoint) {
   RSVDT_TRY(require_ready(ctx, true));
   const int64_t rows = ctx->blk_rows, n = rows * ctx->Nw_eff * ctx->K;
+  if (ctx->capacity) return cap_svd(ctx, before_adjoint != 0);
   if (before_adjoint) {
     RSVDT_TRY(svd_all(ctx, ctx->blk, rows, ctx->Nw_eff, ctx->K, nullptr, ctx->S));
     // StoreU (SourceCode/StoreU.c:15).
@@ -803,6 +1069,14 @@ rsvdt_status rsvdt_get_results(rsvdt_ctx *ctx, double *U, int64_t ldu, double *V
   if (!ctx) return RSVDT_ERR_ARG;
   if (!ctx->have_results) return set_err(ctx, RSVDT_ERR_STATE, "no results yet (call rsvdt_run)");
   const int64_t C = ctx->Nw_eff * ctx->K;
+  if (ctx->capacity) {
+    if ((U && ldu < ctx->U_rows) || (V && ldv < ctx->Nb)) return set_err(ctx, RSVDT_ERR_ARG, "leading dimension too small");
+    if (U) host_u_cols(ctx, nullptr, C, U, ldu);
+    if (V) RSVDT_TRY(block_cols_to_host(ctx, ctx->blk, ctx->Nb, C, nullptr, C, V, ldv));
+    if (S && !cuda_ok(ctx, cudaMemcpy(S, ctx->S, sizeof(double) * C, cudaMemcpyDeviceToHost), "download"))
+      return RSVDT_ERR_CUDA;
+    return RSVDT_OK;
+  }
   auto fetch = [&](const z128 *src, int64_t rows, double *dst, int64_t ld) -> rsvdt_status {
     if (!dst) return RSVDT_OK;
     if (ld < rows) return set_err(ctx, RSVDT_ERR_ARG, "leading dimension too small");
@@ -848,6 +1122,7 @@ rsvdt_status rsvdt_rk4_profile(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_
 rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps, double *y, double *F3) {
   RSVDT_TRY(require_ready(ctx, true));
   if (!y || !F3) return set_err(ctx, RSVDT_ERR_ARG, "null state");
+  if (ctx->capacity) return set_err(ctx, RSVDT_ERR_STATE, "rsvdt_rk4_steps is not available in capacity mode");
   if (ctx->blk_rows != ctx->N) return set_err(ctx, RSVDT_ERR_STATE, "working block must have N rows");
   const int prec = ctx->act_prec;
   const int64_t N = ctx->N, K = ctx->K;
@@ -893,5 +1168,46 @@ rsvdt_status rsvdt_synchronize(rsvdt_ctx *ctx) {
 void *rsvdt_stream(rsvdt_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
 int64_t rsvdt_launch_count(const rsvdt_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+rsvdt_status rsvdt_set_capacity_mode(rsvdt_ctx *ctx, int64_t kc, int32_t u_c64) {
+  if (!ctx) return RSVDT_ERR_ARG;
+  if (kc < 0) return set_err(ctx, RSVDT_ERR_ARG, "chunk size must be non-negative");
+  if (ctx->have_block) return set_err(ctx, RSVDT_ERR_STATE, "set the capacity mode before the sketch");
+  ctx->capacity = true;
+  ctx->cap_kc = kc;
+  ctx->cap_u_c64 = u_c64 ? 1 : 0;
+  ctx->u_host.clear();
+  if (ctx->have_operator) {
+    update_dims(ctx);
+    RSVDT_TRY(ensure_buffers(ctx, ctx->K > 0 ? ctx->K : ctx->par.k));
+  }
+  return RSVDT_OK;
+}
+
+rsvdt_status rsvdt_get_capacity(const rsvdt_ctx *ctx, int64_t *kc) {
+  if (!ctx || !kc) return RSVDT_ERR_ARG;
+  *kc = ctx->capacity ? ctx->Ks : 0;
+  return RSVDT_OK;
+}
+
+rsvdt_status rsvdt_get_result_cols(rsvdt_ctx *ctx, const int64_t *cols, int64_t ncols, double *U, int64_t ldu,
+                                   double *V, int64_t ldv) {
+  if (!ctx) return RSVDT_ERR_ARG;
+  if (!ctx->have_results) return set_err(ctx, RSVDT_ERR_STATE, "no results yet (call rsvdt_run)");
+  const int64_t C = ctx->Nw_eff * ctx->K;
+  if (ncols < 0 || (ncols > 0 && !cols)) return set_err(ctx, RSVDT_ERR_ARG, "invalid column list");
+  for (int64_t j = 0; j < ncols; ++j)
+    if (cols[j] < 0 || cols[j] >= C)
+      return set_err(ctx, RSVDT_ERR_ARG, "column %lld out of range [0, %lld)", (long long)cols[j], (long long)C);
+  if ((U && ldu < ctx->U_rows) || (V && ldv < ctx->Nb)) return set_err(ctx, RSVDT_ERR_ARG, "leading dimension too small");
+  if (U) {
+    if (ctx->capacity)
+      host_u_cols(ctx, cols, ncols, U, ldu);
+    else
+      RSVDT_TRY(block_cols_to_host(ctx, ctx->Ublk, ctx->U_rows, C, cols, ncols, U, ldu));
+  }
+  if (V) RSVDT_TRY(block_cols_to_host(ctx, ctx->capacity ? ctx->blk : ctx->Vblk, ctx->Nb, C, cols, ncols, V, ldv));
+  return RSVDT_OK;
+}
 
 }  // extern "C"

@@ -163,6 +163,16 @@ struct rsvdt_ctx {
 
   // Precision of the running action (rsvdt_precision's C128 or C64).
   int act_prec = 0;
+  // Test vectors held by the RK4 state, ring and forcing slabs (Ks = K, or
+  // the chunk size in capacity mode) and the first of them in the block.
+  int64_t Ks = 0, k0 = 0;
+  // Capacity mode: actions by chunks of cap_kc test vectors written in
+  // place, no ping-pong block, U kept in host memory (per chunk, row layout
+  // [row][iw][kc], complex128 or complex64).
+  bool capacity = false, buf_capacity = false;
+  int64_t cap_kc = 0;
+  int cap_u_c64 = 0;
+  std::vector<std::vector<unsigned char>> u_host;
   // Cached CUDA graphs of G RK4 steps per direction, and their precision.
   cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
   int step_graph_prec[2] = {-1, -1};
@@ -229,5 +239,7 @@ rsvdt_status launch_random(rsvdt_ctx *ctx, z128 *dst, int64_t n, uint64_t seed);
 rsvdt_status launch_convert_to64(rsvdt_ctx *ctx, const z128 *src, z64 *dst, int64_t n);
 rsvdt_status check_finite(rsvdt_ctx *ctx, const z128 *p, int64_t n, bool *ok);
 rsvdt_status transient_removal(rsvdt_ctx *ctx, int dir, int prec, z128 *out);
+rsvdt_status launch_chunk_copy(rsvdt_ctx *ctx, const z128 *src, z128 *dst, int64_t rows, int64_t Nwe, int64_t Kb,
+                               int64_t k0, int64_t Kc, bool gather);
 
 }  // namespace rsvdt

@@ -463,6 +463,34 @@ rsvdt_status svd_all(rsvdt_ctx *ctx, z128 *blk, int64_t rows, int64_t nw, int64_
   return RSVDT_OK;
 }
 
+// ------------------------------------------------------- test-vector chunks
+
+// Columns k0 .. k0+Kc-1 of every frequency of a [row][iw][Kb] block, to or
+// from a [row][iw][Kc] chunk (gather: chunk = block columns; scatter: the
+// reverse). Used by the capacity mode's weights and U store.
+__global__ void k_chunk_copy(const z128 *__restrict__ src, z128 *__restrict__ dst, int64_t rows, int Nwe, int Kb,
+                             int k0, int Kc, int gather) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t total = rows * Nwe * (int64_t)Kc;
+  if (u >= total) return;
+  const int kc = (int)(u % Kc);
+  const int64_t ri = u / Kc;  // row * Nwe + iw
+  const int64_t b = ri * Kb + k0 + kc;
+  if (gather)
+    dst[u] = src[b];
+  else
+    dst[b] = src[u];
+}
+
+rsvdt_status launch_chunk_copy(rsvdt_ctx *ctx, const z128 *src, z128 *dst, int64_t rows, int64_t Nwe, int64_t Kb,
+                               int64_t k0, int64_t Kc, bool gather) {
+  const int th = 256;
+  k_chunk_copy<<<grid_for(rows * Nwe * Kc, th), th, 0, ctx->stream>>>(src, dst, rows, (int)Nwe, (int)Kb, (int)k0,
+                                                                     (int)Kc, gather ? 1 : 0);
+  ctx->launches += 1;
+  return cuda_ok(ctx, cudaGetLastError(), "chunk copy") ? RSVDT_OK : RSVDT_ERR_CUDA;
+}
+
 // ---------------------------------------------------------------- misc
 
 __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
@@ -674,7 +702,9 @@ __global__ void k_galerkin_update(const z128 *__restrict__ V, int64_t N, int Ns1
 // e^{A dT} applied by ResRatio unforced RK4 steps, then the Galerkin
 // correction of each frequency. Writes out[n][iw][k].
 rsvdt_status transient_removal(rsvdt_ctx *ctx, int dir, int prec, z128 *out) {
-  const int64_t N = ctx->N, K = ctx->K, Nw = ctx->Nw, Nwe = ctx->Nw_eff, R = ctx->R;
+  // The ring holds the state's Ks test vectors; they are columns k0.. of out.
+  const int64_t N = ctx->N, K = ctx->Ks, Kb = ctx->K, k0 = ctx->k0, Nw = ctx->Nw, Nwe = ctx->Nw_eff,
+                R = ctx->R;
   const int Ns1 = (int)(Nw + 1);
   if (Ns1 > 32 * 32) return set_err(ctx, RSVDT_ERR_ARG, "Nw too large for transient removal");
   // Buffers: V, MV [N][Ns1]; y1, y2 [N][Nwe]; Mt [Ns1^2]; rhs parts; W.
@@ -739,7 +769,7 @@ rsvdt_status transient_removal(rsvdt_ctx *ctx, int dir, int prec, z128 *out) {
     k_galerkin_solve<<<grid_for(Nwe, 32), 32, 0, ctx->stream>>>(s.G, Ns1, (int)Nwe, ev, W, rhs,
                                                                  ctx->d_flags);
     k_galerkin_update<<<grid_for((int64_t)nY, th), th, 0, ctx->stream>>>(V, N, Ns1, y1, (int)Nwe,
-                                                                         rhs, (int)K, (int)ik, out);
+                                                                         rhs, (int)Kb, (int)(k0 + ik), out);
     ctx->launches += 4;
     if (!cuda_ok(ctx, cudaGetLastError(), "transient removal")) st = RSVDT_ERR_CUDA;
   }

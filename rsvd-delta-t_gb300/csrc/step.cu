@@ -666,11 +666,12 @@ __global__ void k_forcing_init(const StepArgs<Z> P) {
   P.y[t] = zmake<Z>(0, 0);
 }
 
-// Forcing slabs from the working block blk[n][iw][k] (complex128):
-// Fh[s][n][k], pair or plain (see the file comment), in precision Z.
+// Forcing slabs from test vectors k0 .. k0+K-1 of the working block
+// blk[n][iw][kb] (complex128, Kb test vectors): Fh[s][n][k], pair or plain
+// (see the file comment), in precision Z.
 template <class Z>
 __global__ void k_stage_slabs(const z128 *__restrict__ blk, int64_t N, int Nw, int K, int pair,
-                              Z *__restrict__ Fh) {
+                              Z *__restrict__ Fh, int Kb, int k0) {
   const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t NK = N * K;
   if (u >= NK * Nw) return;
@@ -678,19 +679,19 @@ __global__ void k_stage_slabs(const z128 *__restrict__ blk, int64_t N, int Nw, i
   const int64_t r = u - (int64_t)s * NK;
   const int64_t n = r / K;
   const int kc = (int)(r - n * K);
-  const z128 *row = blk + n * (int64_t)Nw * K + kc;
+  const z128 *row = blk + n * (int64_t)Nw * Kb + k0 + kc;
   z128 v;
   if (!pair) {
-    v = row[(int64_t)s * K];
+    v = row[(int64_t)s * Kb];
   } else {
     const int H = Nw / 2;
     if (s == 0) {
       v = row[0];
     } else if (s == Nw - 1) {
-      v = row[(int64_t)H * K];
+      v = row[(int64_t)H * Kb];
     } else {
       const int f = s < H ? s : s - H + 1;
-      const z128 cp = row[(int64_t)f * K], cn = row[(int64_t)(Nw - f) * K];
+      const z128 cp = row[(int64_t)f * Kb], cn = row[(int64_t)(Nw - f) * Kb];
       if (s < H)
         v = zmake<z128>(cp.re + cn.re, cp.im + cn.im);
       else  // i (cp - cn)
@@ -704,7 +705,7 @@ template <class Z>
 static StepArgs<Z> make_args(rsvdt_ctx *ctx, int dir, bool forced) {
   StepArgs<Z> P;
   P.N = ctx->N;
-  P.K = (int)ctx->K;
+  P.K = (int)ctx->Ks;
   P.Nw = (int)ctx->Nw_eff;
   P.pair = ctx->pair ? 1 : 0;
   P.dir = dir;
@@ -806,17 +807,18 @@ static void enqueue_step(rsvdt_ctx *ctx, const StepArgs<Z> &P) {
   for (int s = 1; s <= 4; ++s) launch_stage(s, P, ctx->stream);
 }
 
+// Slabs of the state's Ks test vectors, k0 .. k0+Ks-1 of the working block.
 rsvdt_status stage_forcing_coeffs(rsvdt_ctx *ctx, int prec) {
-  const int64_t total = ctx->N * ctx->Nw_eff * ctx->K;
+  const int64_t total = ctx->N * ctx->Nw_eff * ctx->Ks;
   const int th = 256;
   if (prec == RSVDT_PREC_C64)
     k_stage_slabs<z64><<<grid_for(total, th), th, 0, ctx->stream>>>(ctx->blk, ctx->N, (int)ctx->Nw_eff,
-                                                                     (int)ctx->K, ctx->pair ? 1 : 0,
-                                                                     (z64 *)ctx->Fh);
+                                                                     (int)ctx->Ks, ctx->pair ? 1 : 0,
+                                                                     (z64 *)ctx->Fh, (int)ctx->K, (int)ctx->k0);
   else
     k_stage_slabs<z128><<<grid_for(total, th), th, 0, ctx->stream>>>(ctx->blk, ctx->N, (int)ctx->Nw_eff,
-                                                                      (int)ctx->K, ctx->pair ? 1 : 0,
-                                                                      (z128 *)ctx->Fh);
+                                                                      (int)ctx->Ks, ctx->pair ? 1 : 0,
+                                                                      (z128 *)ctx->Fh, (int)ctx->K, (int)ctx->k0);
   ctx->launches += 1;
   return cuda_ok(ctx, cudaGetLastError(), "forcing slabs") ? RSVDT_OK : RSVDT_ERR_CUDA;
 }
@@ -920,12 +922,13 @@ rsvdt_status profile_steps(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_
 }
 
 // DFT of the sampled period (SourceCode/DFT.c:26-38), FP64 sums:
-// out[n][iw][k] = ResRatio * sum_p ring[p][n][k] * dft[p][iw].
+// out[n][iw][k0 + k] = ResRatio * sum_p ring[p][n][k] * dft[p][iw] for the
+// ring's K test vectors (out holds Kb per frequency).
 template <class Z>
 __global__ void __launch_bounds__(256) k_dft(const Z *__restrict__ ring,
                                              const z128 *__restrict__ dft, int64_t N, int K,
                                              int Nw, int Nwe, double R, z128 *__restrict__ out,
-                                             int32_t *flags) {
+                                             int32_t *flags, int Kb, int k0) {
   const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t total = N * (int64_t)Nwe * K;
   if (u >= total) return;
@@ -943,20 +946,21 @@ __global__ void __launch_bounds__(256) k_dft(const Z *__restrict__ ring,
   s.re *= R;
   s.im *= R;
   if (!isfinite(s.re) || !isfinite(s.im)) atomicOr(flags, 1);
-  out[u] = s;
+  out[(n * Nwe + iw) * Kb + k0 + kc] = s;
 }
 
+// DFT of the ring (the state's Ks test vectors) into columns k0.. of `out`.
 rsvdt_status launch_dft(rsvdt_ctx *ctx, int prec, z128 *out) {
   const int th = 256;
-  const int64_t total = ctx->N * ctx->Nw_eff * ctx->K;
+  const int64_t total = ctx->N * ctx->Nw_eff * ctx->Ks;
   if (prec == RSVDT_PREC_C64)
     k_dft<z64><<<grid_for(total, th), th, 0, ctx->stream>>>(
-        (const z64 *)ctx->ring, ctx->dft, ctx->N, (int)ctx->K, (int)ctx->Nw, (int)ctx->Nw_eff,
-        (double)ctx->R, out, ctx->d_flags);
+        (const z64 *)ctx->ring, ctx->dft, ctx->N, (int)ctx->Ks, (int)ctx->Nw, (int)ctx->Nw_eff,
+        (double)ctx->R, out, ctx->d_flags, (int)ctx->K, (int)ctx->k0);
   else
     k_dft<z128><<<grid_for(total, th), th, 0, ctx->stream>>>(
-        (const z128 *)ctx->ring, ctx->dft, ctx->N, (int)ctx->K, (int)ctx->Nw, (int)ctx->Nw_eff,
-        (double)ctx->R, out, ctx->d_flags);
+        (const z128 *)ctx->ring, ctx->dft, ctx->N, (int)ctx->Ks, (int)ctx->Nw, (int)ctx->Nw_eff,
+        (double)ctx->R, out, ctx->d_flags, (int)ctx->K, (int)ctx->k0);
   ctx->launches += 1;
   if (!cuda_ok(ctx, cudaGetLastError(), "dft")) return RSVDT_ERR_CUDA;
   return RSVDT_OK;

@@ -39,6 +39,7 @@ EXPORTED = [
     "rsvdt_get_results", "rsvdt_rk4_steps", "rsvdt_rk4_reset", "rsvdt_rk4_advance",
     "rsvdt_rk4_profile", "rsvdt_synchronize", "rsvdt_stream", "rsvdt_launch_count",
     "rsvdt_qr_all_freqs_noalloc", "rsvdt_trans_grid", "rsvdt_trans_run",
+    "rsvdt_set_capacity_mode", "rsvdt_get_capacity", "rsvdt_get_result_cols",
     "rsvdt_batch_create", "rsvdt_batch_destroy", "rsvdt_batch_last_error", "rsvdt_batch_add",
     "rsvdt_batch_set_sketch", "rsvdt_batch_random_sketch", "rsvdt_batch_run", "rsvdt_batch_get_results",
     "rsvdt_batch_get_grid", "rsvdt_batch_get_tuning", "rsvdt_batch_launch_count",
@@ -143,6 +144,9 @@ def load_library(path: str | None = None) -> C.CDLL:
         "rsvdt_rk4_advance": (C.c_int, [vp, C.c_int, i64, i64]),
         "rsvdt_rk4_profile": (C.c_int, [vp, C.c_int, i64, i64, d]),
         "rsvdt_qr_all_freqs_noalloc": (C.c_int, [vp, vp, i64, i64, i64, vp, C.c_char_p, i64]),
+        "rsvdt_set_capacity_mode": (C.c_int, [vp, i64, C.c_int32]),
+        "rsvdt_get_capacity": (C.c_int, [vp, P(i64)]),
+        "rsvdt_get_result_cols": (C.c_int, [vp, P(i64), i64, d, i64, d, i64]),
         "rsvdt_trans_grid": (C.c_int, [vp, P(TransParams), P(TransInfo)]),
         "rsvdt_trans_run": (C.c_int, [vp, P(TransParams), d, d, TRANS_SNAPSHOT_FN, TRANS_ESTIMATE_FN, vp,
                                       P(TransInfo)]),
@@ -348,6 +352,29 @@ class Context:
         self._check(self._lib.rsvdt_rk4_profile(self._h, direction, i0, nsteps,
                                                 out.ctypes.data_as(C.POINTER(C.c_double))))
         return out.tolist()
+
+    # -------------------------------------------------------- capacity mode
+    def set_capacity_mode(self, kc: int = 0, u_c64: bool = False) -> None:
+        """Chunked actions, in-place blocks, U in host memory (call before
+        set_operator for problems whose resident buffers would not fit)."""
+        self._check(self._lib.rsvdt_set_capacity_mode(self._h, kc, 1 if u_c64 else 0))
+
+    def capacity_chunk(self) -> int:
+        kc = C.c_int64()
+        self._check(self._lib.rsvdt_get_capacity(self._h, C.byref(kc)))
+        return kc.value
+
+    def get_result_cols(self, cols, U: bool = True, V: bool = True):
+        """Columns (iw*k + ik) of U and V after run()."""
+        g = self.grid()
+        cols = np.ascontiguousarray(cols, dtype=np.int64)
+        Uo = np.zeros((g.Nc, cols.size), dtype=np.complex128, order="F") if U else None
+        Vo = np.zeros((g.Nb, cols.size), dtype=np.complex128, order="F") if V else None
+        dp = C.POINTER(C.c_double)
+        self._check(self._lib.rsvdt_get_result_cols(
+            self._h, _iptr(cols), cols.size, Uo.ctypes.data_as(dp) if U else None, g.Nc,
+            Vo.ctypes.data_as(dp) if V else None, g.Nb))
+        return Uo, Vo
 
     # -------------------------------------------------------- transient run
     @staticmethod
