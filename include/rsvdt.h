@@ -213,6 +213,10 @@ rsvdt_status rsvdt_set_capacity_mode(rsvdt_ctx *ctx, int64_t kc, int32_t u_c64);
 /* Chunk size in use (0 when the context is not in capacity mode). */
 rsvdt_status rsvdt_get_capacity(const rsvdt_ctx *ctx, int64_t *kc);
 
+/* Free and total memory of the current CUDA device, in bytes (for callers
+ * deciding on the capacity mode before they create the buffers). */
+rsvdt_status rsvdt_device_memory(int64_t *free_bytes, int64_t *total_bytes);
+
 /* Columns cols[0..ncols) (indices iw*k + ik) of U (Nc rows) and V (Nb rows)
  * after rsvdt_run, column-major with leading dimensions ldu / ldv; U or V
  * may be NULL. For results too large to fetch whole (e.g. the files of

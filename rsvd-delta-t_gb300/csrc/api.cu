@@ -1184,6 +1184,17 @@ rsvdt_status rsvdt_set_capacity_mode(rsvdt_ctx *ctx, int64_t kc, int32_t u_c64) 
   return RSVDT_OK;
 }
 
+rsvdt_status rsvdt_device_memory(int64_t *free_bytes, int64_t *total_bytes) {
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+    cudaGetLastError();
+    return RSVDT_ERR_CUDA;
+  }
+  if (free_bytes) *free_bytes = (int64_t)fr;
+  if (total_bytes) *total_bytes = (int64_t)tot;
+  return RSVDT_OK;
+}
+
 rsvdt_status rsvdt_get_capacity(const rsvdt_ctx *ctx, int64_t *kc) {
   if (!ctx || !kc) return RSVDT_ERR_ARG;
   *kc = ctx->capacity ? ctx->Ks : 0;

@@ -462,6 +462,22 @@ int main(int argc, char **argv) {
   load_csr(path, &A);
   if (A.rows != A.cols) die("the operator must be square, current size = %lld x %lld", (long long)A.rows,
                             (long long)A.cols);
+  /* Problems whose resident buffers (five spectral blocks, the ring, the
+   * operator and its conjugate transpose) would not fit in device memory
+   * run in the capacity mode. */
+  {
+    int64_t dev_free = 0, dev_total = 0;
+    if (rsvdt_device_memory(&dev_free, &dev_total) == RSVDT_OK) {
+      const double blk = 16.0 * (double)A.rows * (double)p.Nw * (double)p.k;
+      const double resident = 5 * blk + 16.0 * (double)(p.Nw + 1) * (double)A.rows * (double)p.k +
+                              2 * 28.0 * (double)A.nnz;
+      if (resident > 0.9 * (double)dev_free) {
+        check(ctx, rsvdt_set_capacity_mode(ctx, 0, 0), "capacity mode");
+        printf("Capacity mode: the resident buffers (%.1f GB) exceed the free device memory (%.1f GB)\n",
+               resident / 1e9, dev_free / 1e9);
+      }
+    }
+  }
   check(ctx, rsvdt_set_operator(ctx, A.rows, A.rowptr, A.col, A.val), "operator");
   printf("The operator is loaded (N = %lld)\n", (long long)A.rows);
   pb_free(&A);
@@ -516,47 +532,42 @@ int main(int argc, char **argv) {
          "********************************************\n");
   check(ctx, rsvdt_run(ctx), "RSVD-Delta-t");
 
-  /* SaveResults (SourceCode/SaveResults.c:32-92). */
-  const int64_t nwe = g.Nw_eff, ncol = k * nwe;
-  double *U = (double *)malloc(sizeof(double) * 2 * g.Nc * ncol);
-  double *V = (double *)malloc(sizeof(double) * 2 * g.Nb * ncol);
+  /* SaveResults (SourceCode/SaveResults.c:32-92), one file's columns at a
+   * time (a file is N x Nw_eff or N x k; the whole U and V may not fit in
+   * host memory). */
+  const int64_t nwe = g.Nw_eff;
   double *S = (double *)malloc(sizeof(double) * k * nwe);
-  if (!U || !V || !S) die("out of memory");
-  check(ctx, rsvdt_get_results(ctx, U, g.Nc, V, g.Nb, S), "results");
+  if (!S) die("out of memory");
+  check(ctx, rsvdt_get_results(ctx, NULL, 1, NULL, 1, S), "results");
   printf("\nThe results directory: %s\n\n", d.folder);
   char err[512];
   join(path, d.folder, "S_hat");
   if (pb_write_dense_real(path, S, k, nwe, k, err, sizeof err)) die("%s", err);
-  if (d.save_opt == 1) {
-    double *tmp = (double *)malloc(sizeof(double) * 2 * (g.Nc > g.Nb ? g.Nc : g.Nb) * nwe);
-    for (int64_t ik = 0; ik < k; ++ik) {
-      for (int pass = 0; pass < 2; ++pass) {
-        const double *src = pass ? V : U;
-        int64_t rows = pass ? g.Nb : g.Nc;
-        for (int64_t iw = 0; iw < nwe; ++iw)
-          memcpy(tmp + 2 * iw * rows, src + 2 * (iw * k + ik) * rows, sizeof(double) * 2 * rows);
-        char name[128];
-        snprintf(name, sizeof name, "%s%d%s", pass ? "V_hat_k" : "U_hat_k", (int)ik + 1, "_allFreqs");
-        join(path, d.folder, name);
-        if (pb_write_dense(path, tmp, rows, nwe, rows, err, sizeof err)) die("%s", err);
-      }
-    }
-    free(tmp);
-  } else {
-    for (int64_t iw = 0; iw < nwe; ++iw) {
-      char name[128];
-      snprintf(name, sizeof name, "U_hat_Freq%d_allK", (int)iw);
-      join(path, d.folder, name);
-      if (pb_write_dense(path, U + 2 * iw * k * g.Nc, g.Nc, k, g.Nc, err, sizeof err)) die("%s", err);
-      snprintf(name, sizeof name, "V_hat_Freq%d_allK", (int)iw);
-      join(path, d.folder, name);
-      if (pb_write_dense(path, V + 2 * iw * k * g.Nb, g.Nb, k, g.Nb, err, sizeof err)) die("%s", err);
-    }
+  const int64_t per = d.save_opt == 1 ? nwe : k;
+  int64_t *cols = (int64_t *)malloc(sizeof(int64_t) * per);
+  double *Ub = (double *)malloc(sizeof(double) * 2 * g.Nc * per);
+  double *Vb = (double *)malloc(sizeof(double) * 2 * g.Nb * per);
+  if (!cols || !Ub || !Vb) die("out of memory");
+  const int64_t nfiles = d.save_opt == 1 ? k : nwe;
+  for (int64_t f = 0; f < nfiles; ++f) {
+    for (int64_t j = 0; j < per; ++j) cols[j] = d.save_opt == 1 ? j * k + f : f * k + j;
+    check(ctx, rsvdt_get_result_cols(ctx, cols, per, Ub, g.Nc, Vb, g.Nb), "results");
+    char name[128];
+    if (d.save_opt == 1)
+      snprintf(name, sizeof name, "U_hat_k%d_allFreqs", (int)f + 1);
+    else
+      snprintf(name, sizeof name, "U_hat_Freq%d_allK", (int)f);
+    join(path, d.folder, name);
+    if (pb_write_dense(path, Ub, g.Nc, per, g.Nc, err, sizeof err)) die("%s", err);
+    name[0] = 'V';
+    join(path, d.folder, name);
+    if (pb_write_dense(path, Vb, g.Nb, per, g.Nb, err, sizeof err)) die("%s", err);
   }
+  free(cols);
+  free(Ub);
+  free(Vb);
   save_inputs_copy(inputs, d.folder);
   printf("DONE :))\n\n");
-  free(U);
-  free(V);
   free(S);
   rsvdt_destroy(ctx);
   return 0;

@@ -39,7 +39,7 @@ EXPORTED = [
     "rsvdt_get_results", "rsvdt_rk4_steps", "rsvdt_rk4_reset", "rsvdt_rk4_advance",
     "rsvdt_rk4_profile", "rsvdt_synchronize", "rsvdt_stream", "rsvdt_launch_count",
     "rsvdt_qr_all_freqs_noalloc", "rsvdt_trans_grid", "rsvdt_trans_run",
-    "rsvdt_set_capacity_mode", "rsvdt_get_capacity", "rsvdt_get_result_cols",
+    "rsvdt_set_capacity_mode", "rsvdt_get_capacity", "rsvdt_get_result_cols", "rsvdt_device_memory",
     "rsvdt_batch_create", "rsvdt_batch_destroy", "rsvdt_batch_last_error", "rsvdt_batch_add",
     "rsvdt_batch_set_sketch", "rsvdt_batch_random_sketch", "rsvdt_batch_run", "rsvdt_batch_get_results",
     "rsvdt_batch_get_grid", "rsvdt_batch_get_tuning", "rsvdt_batch_launch_count",
@@ -146,6 +146,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "rsvdt_qr_all_freqs_noalloc": (C.c_int, [vp, vp, i64, i64, i64, vp, C.c_char_p, i64]),
         "rsvdt_set_capacity_mode": (C.c_int, [vp, i64, C.c_int32]),
         "rsvdt_get_capacity": (C.c_int, [vp, P(i64)]),
+        "rsvdt_device_memory": (C.c_int, [P(i64), P(i64)]),
         "rsvdt_get_result_cols": (C.c_int, [vp, P(i64), i64, d, i64, d, i64]),
         "rsvdt_trans_grid": (C.c_int, [vp, P(TransParams), P(TransInfo)]),
         "rsvdt_trans_run": (C.c_int, [vp, P(TransParams), d, d, TRANS_SNAPSHOT_FN, TRANS_ESTIMATE_FN, vp,
@@ -320,16 +321,17 @@ class Context:
     def k(self) -> int:
         return int(self._k) if hasattr(self, "_k") else int(self.params.k)
 
-    def get_results(self):
+    def get_results(self, U: bool = True, V: bool = True):
+        """(U, V, S); U or V is None when not requested."""
         g = self.grid()
         ncol = self.k * g.Nw_eff
-        U = np.zeros((g.Nc, ncol), dtype=np.complex128, order="F")
-        V = np.zeros((g.Nb, ncol), dtype=np.complex128, order="F")
+        dp = C.POINTER(C.c_double)
+        Uo = np.zeros((g.Nc, ncol), dtype=np.complex128, order="F") if U else None
+        Vo = np.zeros((g.Nb, ncol), dtype=np.complex128, order="F") if V else None
         S = np.zeros((self.k, g.Nw_eff), dtype=np.float64, order="F")
-        self._check(self._lib.rsvdt_get_results(self._h, U.ctypes.data_as(C.POINTER(C.c_double)), g.Nc,
-                                                V.ctypes.data_as(C.POINTER(C.c_double)), g.Nb,
-                                                S.ctypes.data_as(C.POINTER(C.c_double))))
-        return U, V, S
+        self._check(self._lib.rsvdt_get_results(self._h, Uo.ctypes.data_as(dp) if U else None, g.Nc,
+                                                Vo.ctypes.data_as(dp) if V else None, g.Nb, S.ctypes.data_as(dp)))
+        return Uo, Vo, S
 
     def rk4_steps(self, direction: int, i0: int, nsteps: int, y: np.ndarray, F3: np.ndarray):
         """Advances the host state y, F3 (N x k complex, Fortran order) in place."""

@@ -81,7 +81,7 @@ def build_host(force: bool = False) -> str | None:
     os.makedirs(BIN_DIR, exist_ok=True)
     deps = srcs + [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")] + [LIB_PATH]
     if force or _stale(MAIN_PATH, deps):
-        _run(["gcc", "-O2", "-std=c11", "-Wall", "-I", INCLUDE, "-I", HOST, *srcs, "-o", MAIN_PATH,
+        _run(["gcc", "-O2", "-std=c11", "-fopenmp", "-Wall", "-I", INCLUDE, "-I", HOST, *srcs, "-o", MAIN_PATH,
               "-L", LIB_DIR, "-lrsvdt", "-Wl,-rpath,$ORIGIN/../lib", "-lm"])
     return MAIN_PATH
 
