@@ -268,6 +268,68 @@ def batch_form(count: int = 48, q: int = 0, seed: int = 2024):
     return out
 
 
+def large_precision_form(n: int = 128, k: int = 16, Nw: int = 64, periods: float = 1.0, seed: int = 99):
+    """Precision form on the 3D operator at n^3 (n = 128: N = 10.5M, 14.6M
+    5x5 blocks, k = 16, 64 frequencies, q = 1): variant 1 = complex64 stages
+    with FP32 accumulation, FP64 DFT/QR/SVD and the FP64 sweep (the last
+    adjoint action in complex128); variant 2 = plain complex128. One
+    spectral block is 172 GB, so both run in capacity mode (test vectors in
+    chunks, U in host memory in complex64). Wall time of the whole sequence,
+    per-stage times of one chunk step, and variant 1's gain and first-mode
+    (V) errors against variant 2. `periods` transient periods."""
+    import rsvdt
+    from rsvdt import workloads
+
+    t0 = time.perf_counter()
+    wl = workloads.make_3d(n=n, k=k, Nw=Nw, periods=periods)
+    build_s = time.perf_counter() - t0
+    out = {"workload": f"3D{n}: N={wl.N}, {wl.meta['blocks']} 5x5 blocks, k={k}, Nw={Nw}, q=1, "
+                       f"{periods:g} transient period(s), diagonal W_q = W_f", "build_s": round(build_s, 1)}
+    res = {}
+    for name, prec in (("variant1_c64_fp64_sweep", rsvdt.PREC_C64_REFINE), ("variant2_plain_c128", rsvdt.PREC_C128)):
+        ctx = rsvdt.Context(wl.params(precision=prec))
+        ctx.set_capacity_mode(0, True)
+        ctx.set_operator_bcsr(*wl.bcsr)
+        ctx.set_weight(rsvdt.W_Q_SQRT, wl.weights["W_sqrt"])
+        ctx.set_weight(rsvdt.W_F_SQRT_INV, wl.weights["W_sqrt_inv"])
+        ctx.set_weight(rsvdt.W_Q_SQRT_INV, wl.weights["W_sqrt_inv"])
+        ctx.random_sketch(seed)
+        g = ctx.grid()
+        kc = ctx.capacity_chunk()
+        # One chunk's stage times (the first kc test vectors), complex64 and
+        # complex128 stage kernels as the variant uses them.
+        ctx.rk4_reset(rsvdt.DIRECT)
+        st = [x / 2 for x in ctx.rk4_profile(rsvdt.DIRECT, 1, 2)]
+        ctx.random_sketch(seed)
+        ctx.synchronize()
+        t1 = time.perf_counter()
+        ctx.run()
+        ctx.synchronize()
+        run_s = time.perf_counter() - t1
+        S = ctx.get_results(U=False, V=False)[2]
+        _, V1 = ctx.get_result_cols([iw * k for iw in range(g.Nw_eff)], U=False, V=True)
+        res[name] = (np.asfortranarray(S), V1)
+        out[name] = {"run_s": round(run_s, 1), "chunk_k": kc, "Ns": g.Ns, "Nt": g.Nt,
+                     "steps_per_action": g.Ns + g.Nt, "chunk_stage_ms": [round(x, 3) for x in st]}
+        ctx.close()
+    S1, V1 = res["variant1_c64_fp64_sweep"]
+    S2, V2 = res["variant2_plain_c128"]
+    rel = np.abs(S1 - S2) / S2
+    ang = []
+    for j in range(V1.shape[1]):
+        u, v = V1[:, j], V2[:, j]
+        ph = np.vdot(u, v)
+        ph = ph / abs(ph) if abs(ph) > 0 else 1.0
+        d = np.linalg.norm(u / np.linalg.norm(u) * ph - v / np.linalg.norm(v))
+        ang.append(float(2 * np.arcsin(min(1.0, d / 2))))
+    out["variant1_vs_variant2"] = {"gain_rel_err_max_j<=3": float(rel[:3].max()), "gain_rel_err_max": float(rel.max()),
+                                   "mode1_angle_max_rad": max(ang),
+                                   "speedup": round(out["variant2_plain_c128"]["run_s"] /
+                                                    out["variant1_c64_fp64_sweep"]["run_s"], 3)}
+    out["sigma1_range"] = [float(S2[0].min()), float(S2[0].max())]
+    return out
+
+
 def learned_form(n_train: int = 200, n_held: int = 50, N: int = 2000, seed: int = 77):
     """Learned-sketch form on the Ginzburg-Landau family (N = 2000, k = 10,
     Nw = 16; mu0 in [0.2, 0.45], U in [1.5, 2.5]): the method's own forcing
@@ -355,6 +417,9 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batching-form comparison")
     ap.add_argument("--learned", action="store_true", help="run the learned-sketch experiment (about a minute)")
     ap.add_argument("--ttg-n", type=int, default=32, help="grid of the time-to-gains solves")
+    ap.add_argument("--large-n", type=int, default=0,
+                    help="run the precision form on the n^3 operator in capacity mode (128: the 10.5M-row case)")
+    ap.add_argument("--large-periods", type=float, default=1.0, help="transient periods of the --large-n runs")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -374,13 +439,13 @@ def main():
         dist.init_process_group("nccl")
 
     import rsvdt
-    from rsvdt import workloads
+    from rsvdt import replicas, workloads
 
     wl = workloads.make_3d(n=args.n)
     ctx = rsvdt.Context(wl.params(precision=rsvdt.PREC_C128))
     ctx.set_operator_bcsr(*wl.bcsr)
     g = ctx.grid()
-    ctx.random_sketch(1234 + rank)
+    ctx.random_sketch(replicas.rank_seed(1234, rank))
     b = wl.step_bytes(g.ResRatio)
     fl = wl.step_flops()
     def timed(c, i0, n):
@@ -408,12 +473,9 @@ def main():
     torch.cuda.synchronize()
     clk = clocks.stop()
     launches = ctx.launch_count() - launches0
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(ms, dist, device="cuda")
     ms_step = ms / args.steps
-    value = world * b["step"] / (ms_step * 1e-3) / 1e9
+    value = replicas.whole_job_rate(b["step"], ms_step, world) / 1e9
 
     # Dominant kernel: stage 1 timed launch by launch.
     nprof = 5
@@ -441,7 +503,7 @@ def main():
     # Precision form (complex64 stages, FP32 accumulation) on the same shape.
     ctx64 = rsvdt.Context(wl.params(precision=rsvdt.PREC_C64))
     ctx64.set_operator_bcsr(*wl.bcsr)
-    ctx64.random_sketch(1234 + rank)
+    ctx64.random_sketch(replicas.rank_seed(1234, rank))
     ctx64.rk4_reset(rsvdt.DIRECT)
     ctx64.rk4_advance(rsvdt.DIRECT, 1, 3)
     ms64 = timed(ctx64, 4, args.steps) / args.steps
@@ -458,6 +520,9 @@ def main():
     learned_res = None
     if rank == 0 and args.learned:
         learned_res = learned_form()
+    large = None
+    if rank == 0 and args.large_n:
+        large = large_precision_form(n=args.large_n, periods=args.large_periods)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -510,6 +575,7 @@ def main():
             "time_to_gains": ttg,
             "batching": batching,
             "learned_sketch": learned_res,
+            "precision_form_large": large,
         }
         print(json.dumps(out))
     if dist:
