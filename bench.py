@@ -154,9 +154,10 @@ def time_to_gains(n: int, seed: int = 4321):
     n^3 grid, k = 10, Nw = 32, two transient periods: wall time from the
     first device action to the gains on the host, inputs resident. Plain
     complex128 against the precision form (complex64 stages, FP64 DFT / QR /
-    SVD); the precision form's gain and first-mode errors are measured
-    against the plain result. Each form runs once untimed first (graph
-    capture, lazy allocations)."""
+    SVD) and the refinement form (the same with the last adjoint action in
+    complex128); their gain and first-mode errors are measured against the
+    plain result. Before the timed run each form steps 32 untimed steps in
+    both directions (kernel loading, graph capture)."""
     import rsvdt
     from rsvdt import workloads
 
@@ -171,14 +172,17 @@ def time_to_gains(n: int, seed: int = 4321):
         ctx.set_weight(rsvdt.W_F_SQRT_INV, wl.weights["W_sqrt_inv"])
         ctx.set_weight(rsvdt.W_Q_SQRT_INV, wl.weights["W_sqrt_inv"])
         ctx.random_sketch(seed)
-        ctx.run()
+        for d in (rsvdt.DIRECT, rsvdt.ADJOINT):
+            ctx.rk4_reset(d)
+            ctx.rk4_advance(d, 1, 32)
         ctx.random_sketch(seed)
         ctx.synchronize()
         t0 = time.perf_counter()
         ctx.run()
-        U, V, S = ctx.get_results()
+        S = ctx.get_results(U=False, V=False)[2]
         t = time.perf_counter() - t0
-        res[name] = (U, V, S)
+        U = ctx.get_result_cols([iw * wl.k for iw in range(wl.Nw)], U=True, V=False)[0]
+        res[name] = (U, None, S)
         out[name + "_s"] = round(t, 4)
         ctx.close()
     S0, U0 = res["plain_c128"][2], res["plain_c128"][0]
@@ -190,7 +194,7 @@ def time_to_gains(n: int, seed: int = 4321):
         rel = np.abs(S1 - S0) / S0
         ang = []
         for iw in range(S0.shape[1]):
-            u, v = U0[:, iw * k], U1[:, iw * k]
+            u, v = U0[:, iw], U1[:, iw]
             # Chord-based angle (accurate below 1e-8, where arccos is not).
             ph = np.vdot(u, v)
             ph = ph / abs(ph) if abs(ph) > 0 else 1.0
@@ -236,7 +240,8 @@ def batch_form(count: int = 48, q: int = 0, seed: int = 2024):
     out = {"workload": f"{count} Ginzburg-Landau problems, N {min(p['N'] for p in fam)}..{max(p['N'] for p in fam)} "
                        f"(log-uniform), k in {{6,10,16}}, Nw in {{16,32,64}}, dt = T/4096, q = {q}, seed {seed}",
            "sum_N_k": int(sum(p["N"] * p["k"] for p in fam)), "sequential_plain_c128_s": round(t_seq, 3)}
-    for name, prec in (("batched_c128", rsvdt.PREC_C128), ("batched_c64", rsvdt.PREC_C64)):
+    for name, prec in (("batched_c128", rsvdt.PREC_C128), ("batched_c64", rsvdt.PREC_C64),
+                       ("batched_c64_refine", rsvdt.PREC_C64_REFINE)):
         b = rsvdt.Batch(prec)
         for pr in fam:
             b.add(params(pr, prec), pr["A"])
@@ -265,6 +270,49 @@ def batch_form(count: int = 48, q: int = 0, seed: int = 2024):
                                         "problems_over_1e-3": int(sum(e > 1e-3 for e in errs))}
         out[name + "_tuned"] = {"threads": th, "lanes_per_row": lanes, "ms_per_batched_step": round(ms, 4)}
         b.close()
+    return out
+
+
+def gl1_form(threads: int):
+    """The 500-node Ginzburg-Landau configuration (k = 10, 64 frequencies
+    j*0.1 for j = -32..31, dt = T/4096, one transient period): wall time of
+    the whole sequence on the GPU (plain complex128) for q = 0 and q = 1,
+    the leading gains' deviation from the dense resolvent (numpy, FP64), and
+    the CPU baseline: the C restatement of the same run on `threads` host
+    threads (q = 0)."""
+    import rsvdt
+    from rsvdt import synth, workloads
+
+    out = {"workload": "GL1: N=500 Ginzburg-Landau, k=10, Nw=64, dt=T/4096, one transient period"}
+    wl = workloads.make_gl1(k=10)
+    F = synth.gl_sketch(500, 10, 64)
+    A = wl.csr.toarray()
+    om = np.array([(i if i <= 31 else i - 64) * 0.1 for i in range(64)])
+    sd = np.array([np.linalg.svd(np.linalg.inv(1j * w * np.eye(500) - A), compute_uv=False)[:3] for w in om]).T
+    for q in (0, 1):
+        ctx = rsvdt.Context(rsvdt.default_params(k=10, q=q, Nw=64, w=0.1, dt=wl.dt_in,
+                                                 TransientLength=wl.transient_length, Display=0))
+        ctx.set_operator(wl.csr)
+        ctx.set_sketch(F)
+        ctx.run()
+        ctx.set_sketch(F)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.run()
+        S = ctx.get_results(U=False, V=False)[2]
+        t = time.perf_counter() - t0
+        ctx.close()
+        out[f"gpu_q{q}_s"] = round(t, 4)
+        out[f"q{q}_gain1_vs_dense_max"] = float((np.abs(S[0] - sd[0]) / sd[0]).max())
+    import oracle
+
+    o = oracle.Oracle(wl.csr, 64, 0.1, wl.dt_in, wl.transient_length, threads=threads)
+    t0 = time.perf_counter()
+    o.run(F, 0)
+    out["cpu_baseline_q0"] = {"s": round(time.perf_counter() - t0, 3), "cores": threads, "kind": "port",
+                              "sample": "the whole q = 0 run of the C restatement, OpenMP over test vectors"}
+    out["speedup_q0_vs_cpu"] = round(out["cpu_baseline_q0"]["s"] / out["gpu_q0_s"], 2)
+    o.close()
     return out
 
 
@@ -415,8 +463,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-ttg", action="store_true", help="skip the time-to-gains solves")
     ap.add_argument("--no-batch", action="store_true", help="skip the batching-form comparison")
+    ap.add_argument("--no-gl1", action="store_true", help="skip the 500-node Ginzburg-Landau runs")
     ap.add_argument("--learned", action="store_true", help="run the learned-sketch experiment (about a minute)")
-    ap.add_argument("--ttg-n", type=int, default=32, help="grid of the time-to-gains solves")
+    ap.add_argument("--ttg-n", type=int, default=64, help="grid of the time-to-gains solves")
     ap.add_argument("--large-n", type=int, default=0,
                     help="run the precision form on the n^3 operator in capacity mode (128: the 10.5M-row case)")
     ap.add_argument("--large-periods", type=float, default=1.0, help="transient periods of the --large-n runs")
@@ -520,6 +569,9 @@ def main():
     learned_res = None
     if rank == 0 and args.learned:
         learned_res = learned_form()
+    gl1 = None
+    if rank == 0 and not args.no_gl1:
+        gl1 = gl1_form(min(os.cpu_count() or 1, 10))
     large = None
     if rank == 0 and args.large_n:
         large = large_precision_form(n=args.large_n, periods=args.large_periods)
@@ -575,6 +627,7 @@ def main():
             "time_to_gains": ttg,
             "batching": batching,
             "learned_sketch": learned_res,
+            "gl1": gl1,
             "precision_form_large": large,
         }
         print(json.dumps(out))

@@ -289,6 +289,9 @@ rsvdt_status rsvdt_trans_run(rsvdt_ctx *ctx, const rsvdt_trans_params *tp, doubl
  * running SourceCode/main.c:134-144 for each problem in turn. */
 typedef struct rsvdt_batch rsvdt_batch;
 
+/* precision: RSVDT_PREC_C128, RSVDT_PREC_C64, or RSVDT_PREC_C64_REFINE
+ * (complex64 actions, the last adjoint action of every problem batched in
+ * complex128). */
 rsvdt_status rsvdt_batch_create(int32_t precision, rsvdt_batch **out);
 void rsvdt_batch_destroy(rsvdt_batch *b);
 const char *rsvdt_batch_last_error(const rsvdt_batch *b);

@@ -22,18 +22,21 @@
 using namespace rsvdt;
 
 struct rsvdt_batch {
-  int prec = RSVDT_PREC_C128;
+  int prec = RSVDT_PREC_C128;  // stage precision of the actions (C128 or C64)
+  bool refine = false;         // the last adjoint action in complex128
   cudaStream_t stream = nullptr;
   std::vector<rsvdt_ctx *> probs;
   std::string err;
   int64_t *d_step = nullptr;
   void *d_args[2] = {nullptr, nullptr};  // per direction: nprob argument blocks
+  void *d_args128[2] = {nullptr, nullptr};  // complex128 blocks of the refinement form's last action
   std::vector<unsigned char> h_args;
   int2 *d_work = nullptr;
   int nwork = 0;
   int threads = 0, fs = 0;
   double tuned_ms = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t graph128[2] = {nullptr, nullptr};
   bool ready = false;
   int64_t launches = 0;  // batched stage launches (shared by all problems)
 };
@@ -62,12 +65,17 @@ static bool bcuda(rsvdt_batch *b, cudaError_t e, const char *what) {
 }
 
 static void free_batch_graphs(rsvdt_batch *b) {
-  for (auto &g : b->graph)
-    if (g) {
-      cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+  for (auto *gs : {b->graph, b->graph128})
+    for (int d = 0; d < 2; ++d)
+      if (gs[d]) {
+        cudaGraphExecDestroy(gs[d]);
+        gs[d] = nullptr;
+      }
 }
+
+// Argument blocks and graphs of the actions in precision `prec`.
+static void **args_for(rsvdt_batch *b, int prec) { return prec == b->prec ? b->d_args : b->d_args128; }
+static cudaGraphExec_t *graphs_for(rsvdt_batch *b, int prec) { return prec == b->prec ? b->graph : b->graph128; }
 
 // Work list (problem, tile) for a launch shape.
 static rsvdt_status build_work(rsvdt_batch *b, int threads, int fs) {
@@ -88,27 +96,29 @@ static rsvdt_status build_work(rsvdt_batch *b, int threads, int fs) {
 
 // Argument blocks of every problem for direction d; rend[p] = 0 leaves a
 // problem out of this action.
-static rsvdt_status upload_args(rsvdt_batch *b, int d, const std::vector<int64_t> &rend) {
-  const size_t sz = step_args_size(b->prec);
+static rsvdt_status upload_args(rsvdt_batch *b, int d, const std::vector<int64_t> &rend, int prec) {
+  const size_t sz = step_args_size(prec);
   b->h_args.resize(sz * b->probs.size());
   for (size_t p = 0; p < b->probs.size(); ++p)
-    fill_step_args(b->probs[p], d, b->prec, rend[p], b->d_step, b->h_args.data() + p * sz);
-  if (!bcuda(b, cudaMemcpyAsync(b->d_args[d], b->h_args.data(), b->h_args.size(), cudaMemcpyHostToDevice, b->stream),
+    fill_step_args(b->probs[p], d, prec, rend[p], b->d_step, b->h_args.data() + p * sz);
+  if (!bcuda(b, cudaMemcpyAsync(args_for(b, prec)[d], b->h_args.data(), b->h_args.size(), cudaMemcpyHostToDevice,
+                                b->stream),
              "arguments"))
     return RSVDT_ERR_CUDA;
   // The host buffer is reused at the next action: wait for the copy.
   return bcuda(b, cudaStreamSynchronize(b->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
 }
 
-static rsvdt_status capture(rsvdt_batch *b, int d) {
+static rsvdt_status capture(rsvdt_batch *b, int d, int prec) {
   cudaGraph_t g;
   if (!bcuda(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture"))
     return RSVDT_ERR_CUDA;
   for (int s = 0; s < kBatchGraphSteps; ++s)
-    launch_batched_step(b->stream, b->prec, b->d_args[d], b->d_work, b->nwork, b->threads, b->fs, b->d_step);
+    launch_batched_step(b->stream, prec, args_for(b, prec)[d], b->d_work, b->nwork, b->threads, b->fs, b->d_step);
   if (!bcuda(b, cudaStreamEndCapture(b->stream, &g), "end capture")) return RSVDT_ERR_CUDA;
-  if (!bcuda(b, cudaGraphInstantiate(&b->graph[d], g, 0), "graph instantiate")) return RSVDT_ERR_CUDA;
+  const cudaError_t e = cudaGraphInstantiate(&graphs_for(b, prec)[d], g, 0);
   cudaGraphDestroy(g);
+  if (!bcuda(b, e, "graph instantiate")) return RSVDT_ERR_CUDA;
   return RSVDT_OK;
 }
 
@@ -152,34 +162,38 @@ static rsvdt_status autotune(rsvdt_batch *b, int d) {
   return build_work(b, bt, bf);
 }
 
-// One action (direct d = 1 or adjoint d = 0) of every problem in `mask`.
-static rsvdt_status batch_action(rsvdt_batch *b, int d, const std::vector<char> &mask) {
+// One action (direct d = 1 or adjoint d = 0) of every problem in `mask`,
+// stages in precision `prec`.
+static rsvdt_status batch_action(rsvdt_batch *b, int d, const std::vector<char> &mask, int prec) {
   const size_t np = b->probs.size();
   std::vector<int64_t> rend(np, 0);
   int64_t maxrend = 0;
   for (size_t p = 0; p < np; ++p) {
     if (!mask[p]) continue;
+    b->probs[p]->act_prec = prec;
     rsvdt_status st = from_ctx(b, p, action_prepare(b->probs[p], d, &rend[p]));
     if (st) return st;
     maxrend = std::max(maxrend, rend[p]);
   }
-  rsvdt_status st = upload_args(b, d, rend);
+  rsvdt_status st = upload_args(b, d, rend, prec);
   if (st) return st;
   if (!b->threads) {
     st = autotune(b, d);
     if (st) return st;
     // Re-initialise y and the starting forcing after the timed steps.
     for (size_t p = 0; p < np; ++p)
-      if (mask[p] && (st = from_ctx(b, p, launch_forcing_init(b->probs[p], d, b->prec)))) return st;
+      if (mask[p] && (st = from_ctx(b, p, launch_forcing_init(b->probs[p], d, prec)))) return st;
   }
-  if (!b->graph[d] && (st = capture(b, d))) return st;
+  cudaGraphExec_t *gs = graphs_for(b, prec);
+  if (!gs[d] && (st = capture(b, d, prec))) return st;
   launch_set_step(b->stream, b->d_step, 1);
   for (int64_t s = 0; s < maxrend; s += kBatchGraphSteps)
-    if (!bcuda(b, cudaGraphLaunch(b->graph[d], b->stream), "graph launch")) return RSVDT_ERR_CUDA;
+    if (!bcuda(b, cudaGraphLaunch(gs[d], b->stream), "graph launch")) return RSVDT_ERR_CUDA;
   if (!bcuda(b, cudaGetLastError(), "batched steps")) return RSVDT_ERR_CUDA;
   b->launches += 1 + (maxrend + kBatchGraphSteps - 1) / kBatchGraphSteps * kBatchGraphSteps * 4;
   for (size_t p = 0; p < np; ++p)
     if (mask[p] && (st = from_ctx(b, p, action_finish(b->probs[p], d)))) return st;
+  for (size_t p = 0; p < np; ++p) b->probs[p]->act_prec = b->prec;
   return RSVDT_OK;
 }
 
@@ -189,9 +203,10 @@ rsvdt_status rsvdt_batch_create(int32_t precision, rsvdt_batch **out) {
   if (!out) return RSVDT_ERR_ARG;
   rsvdt_batch *b = new rsvdt_batch();
   *out = b;
-  if (precision != RSVDT_PREC_C128 && precision != RSVDT_PREC_C64)
+  if (precision != RSVDT_PREC_C128 && precision != RSVDT_PREC_C64 && precision != RSVDT_PREC_C64_REFINE)
     return bfail(b, RSVDT_ERR_ARG, "unknown precision %d", (int)precision);
-  b->prec = precision;
+  b->prec = base_precision(precision);
+  b->refine = precision == RSVDT_PREC_C64_REFINE;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
     cudaGetLastError();
@@ -208,6 +223,8 @@ void rsvdt_batch_destroy(rsvdt_batch *b) {
   free_batch_graphs(b);
   for (auto *c : b->probs) rsvdt_destroy(c);
   for (auto p : b->d_args)
+    if (p) cudaFree(p);
+  for (auto p : b->d_args128)
     if (p) cudaFree(p);
   if (b->d_work) cudaFree(b->d_work);
   if (b->d_step) cudaFree(b->d_step);
@@ -271,6 +288,12 @@ rsvdt_status rsvdt_batch_run(rsvdt_batch *b) {
       p = nullptr;
       if (!bcuda(b, cudaMalloc(&p, step_args_size(b->prec) * np), "arguments")) return RSVDT_ERR_OOM;
     }
+    for (auto &p : b->d_args128) {
+      if (p) cudaFree(p);
+      p = nullptr;
+      if (b->refine && !bcuda(b, cudaMalloc(&p, step_args_size(RSVDT_PREC_C128) * np), "arguments"))
+        return RSVDT_ERR_OOM;
+    }
     if (b->threads) {
       rsvdt_status st = build_work(b, b->threads, b->fs);
       if (st) return st;
@@ -281,20 +304,21 @@ rsvdt_status rsvdt_batch_run(rsvdt_batch *b) {
   int64_t maxq = 0;
   for (auto *c : b->probs) maxq = std::max(maxq, c->par.q);
   rsvdt_status st;
-  if ((st = batch_action(b, 1, all))) return st;  // SourceCode/main.c:134
+  if ((st = batch_action(b, 1, all, b->prec))) return st;  // SourceCode/main.c:134
   for (int64_t iq = 0; iq < maxq; ++iq) {         // SourceCode/PowerIterationRK4.c:20-29
     std::vector<char> m(np);
     for (size_t p = 0; p < np; ++p) m[p] = b->probs[p]->par.q > iq;
     for (size_t p = 0; p < np; ++p)
       if (m[p] && (st = from_ctx(b, p, rsvdt_qr_all_freqs(b->probs[p])))) return st;
-    if ((st = batch_action(b, 0, m))) return st;
+    if ((st = batch_action(b, 0, m, b->prec))) return st;
     for (size_t p = 0; p < np; ++p)
       if (m[p] && (st = from_ctx(b, p, rsvdt_qr_all_freqs(b->probs[p])))) return st;
-    if ((st = batch_action(b, 1, m))) return st;
+    if ((st = batch_action(b, 1, m, b->prec))) return st;
   }
   for (size_t p = 0; p < np; ++p)
     if ((st = from_ctx(b, p, rsvdt_svd_all_freqs(b->probs[p], 1)))) return st;
-  if ((st = batch_action(b, 0, all))) return st;  // SourceCode/main.c:142
+  // SourceCode/main.c:142; the refinement form's FP64 sweep runs it in complex128.
+  if ((st = batch_action(b, 0, all, b->refine ? RSVDT_PREC_C128 : b->prec))) return st;
   for (size_t p = 0; p < np; ++p)
     if ((st = from_ctx(b, p, rsvdt_svd_all_freqs(b->probs[p], 0)))) return st;
   return bcuda(b, cudaStreamSynchronize(b->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;

@@ -86,6 +86,35 @@ def test_batch_precision_form_close_to_plain(built_lib):
     b.close()
 
 
+def test_batch_refinement_form(built_lib):
+    """Refinement form in a batch: complex64 actions, the last adjoint
+    action of every problem in complex128 (lockstep, its own graph): the
+    gains come closer to the plain form's than the all-complex64 batch's,
+    and equal the single-context refinement form's."""
+    import rsvdt
+    fam = family()
+    res = {}
+    for prec in (rsvdt.PREC_C64, rsvdt.PREC_C64_REFINE):
+        b = rsvdt.Batch(prec)
+        for pr in fam:
+            i = b.add(params_of(rsvdt, pr), pr["A"])
+            b.set_sketch(i, pr["F"])
+        b.run()
+        res[prec] = [b.get_results(i)[2] for i in range(len(fam))]
+        b.close()
+    e64, eref = [], []
+    for i, pr in enumerate(fam):
+        _, _, Sr = solve_alone(rsvdt, pr)
+        _, _, Sa = solve_alone(rsvdt, pr, rsvdt.PREC_C64_REFINE)
+        e64.append((np.abs(res[rsvdt.PREC_C64][i][0] - Sr[0]) / Sr[0]).max())
+        eref.append((np.abs(res[rsvdt.PREC_C64_REFINE][i][0] - Sr[0]) / Sr[0]).max())
+        # Same arithmetic as the single context up to the batched stages'
+        # summation order (complex64 sums: 1e-6).
+        assert (np.abs(res[rsvdt.PREC_C64_REFINE][i] - Sa) / Sa).max() < 1e-5, i
+    print("leading-gain errors, complex64 batch:", max(e64), "refinement batch:", max(eref))
+    assert max(eref) < max(e64)
+
+
 def test_batch_errors(built_lib):
     import rsvdt
     b = rsvdt.Batch()
