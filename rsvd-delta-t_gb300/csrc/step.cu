@@ -288,19 +288,6 @@ __device__ __forceinline__ void st_chunk(Z *p, const Z (&v)[KP]) {
 
 static const int kRowThreads = 128;
 
-// Bulk prefetch of the bytes [a, b) into L2 (cp.async.bulk.prefetch, no
-// shared memory, nothing waits on it): the inner 16-byte-aligned part, in
-// requests of at most 1 MB.
-__device__ __forceinline__ void prefetch_l2_range(const void *a, const void *b) {
-  uintptr_t s = ((uintptr_t)a + 15) & ~(uintptr_t)15;
-  const uintptr_t e = (uintptr_t)b & ~(uintptr_t)15;
-  while (s < e) {
-    const uint32_t n = (uint32_t)((e - s) < ((uintptr_t)1 << 20) ? (e - s) : ((uintptr_t)1 << 20));
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(s), "r"(n) : "memory");
-    s += n;
-  }
-}
-
 // One lane per (5-row block row, group of KP test vectors). The L = K/KP
 // lanes of a block row fetch each gathered k-vector row together, one
 // 16-byte chunk each, so a row is one contiguous access instead of five
@@ -330,22 +317,6 @@ __global__ void __launch_bounds__(kRowThreads) k_bstage(const StepArgs<Z> P) {
       }
     }
     __syncthreads();
-  }
-  if (S != 1 && threadIdx.x == 0) {
-    // Stages 2-4 stream this block's operator blocks and state rows once:
-    // request all of them up front so that they are in flight together.
-    const int64_t nbr = P.N / 5;
-    const int64_t b0 = (int64_t)blockIdx.x * (kRowThreads / 32) * BPW;
-    const int64_t b1 = b0 + (kRowThreads / 32) * BPW < nbr ? b0 + (kRowThreads / 32) * BPW : nbr;
-    if (b0 < b1) {
-      const int32_t j0 = __ldg(P.rowptr + b0), j1 = __ldg(P.rowptr + b1);
-      prefetch_l2_range(P.val + (int64_t)j0 * 25, P.val + (int64_t)j1 * 25);
-      const int64_t e0 = b0 * 5 * K, e1 = b1 * 5 * K;
-      const Z *addp = (S == 4) ? P.F3 : P.F2;
-      prefetch_l2_range(addp + e0, addp + e1);
-      prefetch_l2_range(P.acc + e0, P.acc + e1);
-      if (S != 4) prefetch_l2_range(P.y + e0, P.y + e1);
-    }
   }
   if (sub >= BPW || br >= P.N / 5) return;
   if (S == 1 && br == 0 && q == 0) P.step[1] = i;
