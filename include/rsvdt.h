@@ -213,6 +213,14 @@ rsvdt_status rsvdt_set_capacity_mode(rsvdt_ctx *ctx, int64_t kc, int32_t u_c64);
 /* Chunk size in use (0 when the context is not in capacity mode). */
 rsvdt_status rsvdt_get_capacity(const rsvdt_ctx *ctx, int64_t *kc);
 
+/* Lanes per (row, test vector) of the RK4 stages: 1 = one thread per row
+ * (the stage kernels for large problems), 2 / 4 / 8 = that many lanes
+ * splitting a row's nonzeros and forcing slabs (the batched stage kernel,
+ * for small problems), 0 = chosen from the problem size (default). The
+ * results agree to rounding (summation order). */
+rsvdt_status rsvdt_set_lanes_per_row(rsvdt_ctx *ctx, int32_t lanes);
+int32_t rsvdt_get_lanes_per_row(const rsvdt_ctx *ctx);
+
 /* Free and total memory of the current CUDA device, in bytes (for callers
  * deciding on the capacity mode before they create the buffers). */
 rsvdt_status rsvdt_device_memory(int64_t *free_bytes, int64_t *total_bytes);

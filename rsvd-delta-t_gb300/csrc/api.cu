@@ -62,11 +62,12 @@ void dfree(rsvdt_ctx *ctx, void *p) {
 // ------------------------------------------------------------ helpers
 
 static void free_graphs(rsvdt_ctx *ctx) {
-  for (auto &g : ctx->step_graph)
-    if (g) {
-      cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+  for (auto *gs : {ctx->step_graph, ctx->small_graph})
+    for (int d = 0; d < 2; ++d)
+      if (gs[d]) {
+        cudaGraphExecDestroy(gs[d]);
+        gs[d] = nullptr;
+      }
 }
 
 static bool upload(rsvdt_ctx *ctx, void *dst, const void *src, size_t bytes) {
@@ -1183,6 +1184,16 @@ rsvdt_status rsvdt_set_capacity_mode(rsvdt_ctx *ctx, int64_t kc, int32_t u_c64) 
   }
   return RSVDT_OK;
 }
+
+rsvdt_status rsvdt_set_lanes_per_row(rsvdt_ctx *ctx, int32_t lanes) {
+  if (!ctx) return RSVDT_ERR_ARG;
+  if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8)
+    return set_err(ctx, RSVDT_ERR_ARG, "lanes per row must be 0 (automatic), 1, 2, 4 or 8, not %d", (int)lanes);
+  ctx->lanes_override = lanes;
+  return RSVDT_OK;
+}
+
+int32_t rsvdt_get_lanes_per_row(const rsvdt_ctx *ctx) { return ctx ? step_lanes(ctx) : 0; }
 
 rsvdt_status rsvdt_device_memory(int64_t *free_bytes, int64_t *total_bytes) {
   size_t fr = 0, tot = 0;

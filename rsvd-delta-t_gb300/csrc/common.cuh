@@ -176,6 +176,15 @@ struct rsvdt_ctx {
   // Cached CUDA graphs of G RK4 steps per direction, and their precision.
   cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
   int step_graph_prec[2] = {-1, -1};
+  // Small-problem stepping on the batched stage kernel (step.cu:
+  // step_lanes): lanes per row (0 = chosen from the size), the argument
+  // blocks of both directions, the work list and the cached graphs.
+  int lanes_override = 0;
+  void *small_args = nullptr;
+  int2 *small_work = nullptr;
+  int small_nwork = 0;
+  cudaGraphExec_t small_graph[2] = {nullptr, nullptr};
+  int small_graph_key[2] = {-1, -1};
   int64_t step_graph_len = 0;
 
   std::vector<void *> allocations;
@@ -222,6 +231,7 @@ bool launch_batched_step(cudaStream_t st, int prec, const void *args, const int2
 void launch_set_step(cudaStream_t st, int64_t *step, int64_t i);
 rsvdt_status launch_unforced_steps(rsvdt_ctx *ctx, int dir, z128 *cols, int64_t ncols,
                                    int64_t nsteps);
+int step_lanes(const rsvdt_ctx *ctx);
 rsvdt_status launch_trans_steps(rsvdt_ctx *ctx, double dt, z128 *y, z128 *work, int64_t nsteps,
                                 cudaGraphExec_t *graph);
 // dense.cu

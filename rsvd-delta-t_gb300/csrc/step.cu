@@ -874,7 +874,90 @@ static rsvdt_status run_steps_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t nst
   return RSVDT_OK;
 }
 
+// Lanes per (row, test vector) for a context's stepping: 1 runs the stage
+// kernels above; 2, 4 or 8 runs the batched stage kernel (below) as a
+// batch of one, whose FS lanes split a row's nonzeros and forcing slabs.
+// A small problem (few rows x test vectors, e.g. the 500-node
+// Ginzburg-Landau case) is bound by the dependent-load chain of one
+// thread's forcing synthesis, which the split shortens FS times; the lanes
+// are chosen so that rows x test vectors x FS is about 2^17 threads.
+int step_lanes(const rsvdt_ctx *ctx) {
+  if (ctx->lanes_override > 0) return ctx->lanes_override;
+  const int64_t nk = ctx->N * ctx->Ks;
+  int fs = 1;
+  while (fs < 8 && nk * fs * 2 <= ((int64_t)1 << 17)) fs *= 2;
+  return fs;
+}
+
+static const int kSmallThreads = 128;
+
+static rsvdt_status run_steps_small(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_t nsteps, int fs) {
+  const int d = dir ? 1 : 0;
+  const size_t asz = step_args_size(RSVDT_PREC_C128);  // the larger of the two
+  if (!ctx->small_args) {
+    ctx->small_args = dalloc(ctx, 2 * asz);
+    if (!ctx->small_args) return set_err(ctx, RSVDT_ERR_OOM, "argument block allocation failed");
+  }
+  const int64_t nk = ctx->N * ctx->Ks;
+  const int tiles = (int)((nk * fs + kSmallThreads - 1) / kSmallThreads);
+  if (ctx->small_nwork != tiles) {
+    std::vector<int2> w((size_t)tiles);
+    for (int t = 0; t < tiles; ++t) w[(size_t)t] = make_int2(0, t);
+    dfree(ctx, ctx->small_work);
+    ctx->small_work = (int2 *)dalloc(ctx, sizeof(int2) * (size_t)tiles);
+    if (!ctx->small_work) return set_err(ctx, RSVDT_ERR_OOM, "work list allocation failed");
+    if (!cuda_ok(ctx, cudaMemcpy(ctx->small_work, w.data(), sizeof(int2) * (size_t)tiles, cudaMemcpyHostToDevice),
+                 "work list"))
+      return RSVDT_ERR_CUDA;
+    ctx->small_nwork = tiles;
+    for (auto &g : ctx->small_graph)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+  }
+  // The argument block of this direction (the step counter is the
+  // context's own; no last step).
+  unsigned char host[sizeof(StepArgs<z128>)];
+  fill_step_args(ctx, d, prec, INT64_MAX, ctx->d_step, host);
+  void *dargs = (unsigned char *)ctx->small_args + d * asz;
+  if (!cuda_ok(ctx, cudaMemcpyAsync(dargs, host, step_args_size(prec), cudaMemcpyHostToDevice, ctx->stream), "args"))
+    return RSVDT_ERR_CUDA;
+  launch_set_step(ctx->stream, ctx->d_step, i0);
+  ctx->launches += 1;
+  int64_t done = 0;
+  if (nsteps >= kGraphSteps) {
+    cudaGraphExec_t &ge = ctx->small_graph[d];
+    const int key = prec * 16 + fs;
+    if (ge && ctx->small_graph_key[d] != key) {
+      cudaGraphExecDestroy(ge);
+      ge = nullptr;
+    }
+    if (!ge) {
+      cudaGraph_t g;
+      if (!cuda_ok(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "begin capture"))
+        return RSVDT_ERR_CUDA;
+      for (int64_t s = 0; s < kGraphSteps; ++s)
+        launch_batched_step(ctx->stream, prec, dargs, ctx->small_work, tiles, kSmallThreads, fs, ctx->d_step);
+      if (!cuda_ok(ctx, cudaStreamEndCapture(ctx->stream, &g), "end capture")) return RSVDT_ERR_CUDA;
+      const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      if (!cuda_ok(ctx, e, "graph instantiate")) return RSVDT_ERR_CUDA;
+      ctx->small_graph_key[d] = key;
+    }
+    for (; done + kGraphSteps <= nsteps; done += kGraphSteps)
+      if (!cuda_ok(ctx, cudaGraphLaunch(ge, ctx->stream), "graph launch")) return RSVDT_ERR_CUDA;
+  }
+  for (; done < nsteps; ++done)
+    launch_batched_step(ctx->stream, prec, dargs, ctx->small_work, tiles, kSmallThreads, fs, ctx->d_step);
+  ctx->launches += 4 * nsteps;
+  if (!cuda_ok(ctx, cudaGetLastError(), "rk4 steps")) return RSVDT_ERR_CUDA;
+  return RSVDT_OK;
+}
+
 rsvdt_status run_steps(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_t nsteps, bool) {
+  const int fs = step_lanes(ctx);
+  if (fs > 1) return run_steps_small(ctx, dir, prec, i0, nsteps, fs);
   if (prec == RSVDT_PREC_C64) return run_steps_t<z64>(ctx, dir, i0, nsteps);
   return run_steps_t<z128>(ctx, dir, i0, nsteps);
 }

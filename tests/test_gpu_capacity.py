@@ -23,11 +23,12 @@ def gl_problem():
     return A, dict(w=0.1, Nw=16, dt=0.15, TransientLength=2 * np.pi / 0.1)
 
 
-def ctx_for(cfg, k, q, tr, prec=0, capacity=None, A=None, bcsr=None, weights=()):
+def ctx_for(cfg, k, q, tr, prec=0, capacity=None, A=None, bcsr=None, weights=(), lanes=0):
     import rsvdt
     p = rsvdt.default_params(k=k, q=q, Nw=cfg["Nw"], w=cfg["w"], dt=cfg["dt"], TransientLength=cfg["TransientLength"],
                              TransientRemoval=int(tr), precision=prec, Display=0)
     ctx = rsvdt.Context(p)
+    ctx.set_lanes_per_row(lanes)
     if capacity is not None:
         ctx.set_capacity_mode(*capacity)
     if bcsr is not None:
@@ -92,14 +93,15 @@ def test_chunked_weights_and_complex64_u(built_lib):
 
 @pytest.mark.parametrize("prec", [0, 1])
 def test_chunked_block_operator(built_lib, prec):
-    """5x5 block-CSR operator: the k = 2 row kernels per chunk against the
-    k = 4 kernels of the resident run, both precisions."""
+    """5x5 block-CSR operator: the k = 2 block-row kernels per chunk against
+    the k = 4 kernels of the resident run, both precisions (one lane per
+    row: the kernels of large problems)."""
     br, bc, bl = synth.op3d_blocks(n=4, shift=0.5, seed=3)
     cfg = dict(w=0.5, Nw=8, dt=0.05, TransientLength=2 * np.pi / 0.5)
     k = 4
     F = synth.complex_normal(br.size * 5 - 5, k * 8, 9)
-    (U0, V0, S0), _, _, _ = solve(cfg, F, k, 1, False, bcsr=(br, bc, bl), prec=prec)
-    (U1, V1, S1), used, _, _ = solve(cfg, F, k, 1, False, bcsr=(br, bc, bl), prec=prec, capacity=(2, False))
+    (U0, V0, S0), _, _, _ = solve(cfg, F, k, 1, False, bcsr=(br, bc, bl), prec=prec, lanes=1)
+    (U1, V1, S1), used, _, _ = solve(cfg, F, k, 1, False, bcsr=(br, bc, bl), prec=prec, capacity=(2, False), lanes=1)
     tol = 1e-12 if prec == 0 else 1e-5  # complex64 sums in another kernel's order
     assert used == 2
     assert np.abs(S1 - S0).max() <= tol * S0.max()

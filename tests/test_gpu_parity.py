@@ -148,6 +148,28 @@ def test_plain_forcing_paths_match_oracle(built_lib, case):
         ctx.close()
 
 
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
+def test_lane_split_stepping_matches_oracle(built_lib, lanes):
+    """The stepping of one context with 1 lane per (row, test vector) (the
+    CSR stage kernels) and with 2, 4, 8 lanes splitting the nonzeros and
+    forcing slabs (the batched stage kernel as a batch of one): both
+    directions, transient removal on, against the oracle."""
+    A, cfg = small_gl()
+    k = 3
+    for direction in (1, 0):
+        ctx = make_ctx(A, cfg, k=k, tr=True)
+        ctx.set_lanes_per_row(lanes)
+        assert ctx.lanes_per_row() == lanes
+        g = ctx.grid()
+        F = synth.complex_normal(A.shape[0], k * g.Nw_eff, 41)
+        ctx.set_sketch(F)
+        ctx.action(direction)
+        Y = ctx.get_block()
+        Yo = make_oracle(A, cfg, tr=True).ts_action(direction, F)
+        assert rel(Y, Yo) < 1e-9
+        ctx.close()
+
+
 def test_qr_and_svd_match_oracle(built_lib):
     A, cfg = small_gl()
     k = 4
@@ -231,15 +253,21 @@ def test_weights_match_oracle(built_lib):
     ctx.close()
 
 
-def test_bcsr_matches_csr_and_oracle(built_lib):
+@pytest.mark.parametrize("lanes", [1, 0])
+def test_bcsr_matches_csr_and_oracle(built_lib, lanes):
     """Block-CSR operator (3D five-field shape, 4^3 grid) against the same
-    operator as CSR on the GPU and in the oracle."""
+    operator as CSR on the GPU and in the oracle; lanes = 1 runs the 5x5
+    block-row kernels, 0 the automatic choice (the lane-split kernel at this
+    size)."""
     br, bc, bl = synth.op3d_blocks(n=4, shift=0.5, seed=3)
     Acsr = synth.bcsr_to_csr(br, bc, bl)
     cfg = dict(w=0.5, Nw=8, dt=0.05, TransientLength=2 * np.pi / 0.5)
     k = 2
     ctx_b = make_ctx(None, cfg, k=k, bcsr=(br, bc, bl))
     ctx_c = make_ctx(Acsr, cfg, k=k)
+    ctx_b.set_lanes_per_row(lanes)
+    ctx_c.set_lanes_per_row(lanes)
+    assert ctx_b.lanes_per_row() == (1 if lanes == 1 else 8)
     g = ctx_b.grid()
     F = synth.complex_normal(Acsr.shape[0], k * g.Nw_eff, 9)
     for d in (1, 0):
