@@ -434,6 +434,49 @@ def learned_form(n_train: int = 200, n_held: int = 50, N: int = 2000, seed: int 
     return out
 
 
+def learned3d_form(n: int = 48, n_train: int = 24, n_held: int = 8, seed: int = 91):
+    """Learned-sketch form on the 3D half of the family: the five-field
+    operator at n^3 (n = 48: N = 552,960) over Re in [500, 2000] and a
+    uniform reaction term mu0 in [0.2, 0.45], k = 4, Nw = 16. Training data:
+    the method's own forcing modes (complex64, q = 1) at n_train seeded
+    points; POD basis r = 64 by the method of snapshots; network 3 -> 4 x 256
+    GELU -> 2 r k trained on the GPU. At n_held held-out points: q = 0 from
+    the learned sketch against q = 0, 1, 2 from random sketches, all in the
+    refinement form, gains against a q = 3 solve."""
+    import rsvdt
+    from rsvdt import learned
+
+    fam = learned.Family3D(n=n, k=4, Nw=16)
+    t0 = time.perf_counter()
+    _ = fam.shift  # the family's spectral shift (RK4 growth rate at the least stable corner)
+    t_shift = time.perf_counter() - t0
+    train = fam.points(n_train, seed=seed)
+    held = fam.points(n_held, seed=seed + 1)
+    res, t_data = learned.solve_batch(fam, train, q=1, precision=rsvdt.PREC_C64, seed=seed * 10)
+    ls = learned.LearnedSketch(fam, r=64, hidden=256, depth=4, seed=1)
+    t0 = time.perf_counter()
+    ls.fit(train, [V for (_, V, _) in res], steps=3000, batch=128, lr=1e-3)
+    t_fit = time.perf_counter() - t0
+    res = None
+    prec = rsvdt.PREC_C64_REFINE
+    ref, t_ref = learned.solve_batch(fam, held, q=3, precision=prec, seed=seed * 20)
+    out = {"workload": f"3D family {n}^3 (N={fam.N}), Re in [500, 2000], mu0 in [0.2, 0.45], k=4, Nw=16; "
+                       f"{n_train} training / {n_held} held-out points", "family_shift": round(fam.shift, 6),
+           "shift_s": round(t_shift, 2), "training_data_s": round(t_data, 2), "fit_s": round(t_fit, 2),
+           "train_s_on_gpu": round(ls.train_seconds, 2), "pod_energy_r64": round(ls.pod_energy, 6),
+           "final_loss": ls.final_loss, "reference_q3_s": round(t_ref, 2)}
+    sk = [ls.sketch(p) for p in held]
+    runs = {"learned_q0": (0, sk)}
+    for q in (0, 1, 2):
+        runs[f"random_q{q}"] = (q, None)
+    for name, (q, s_) in runs.items():
+        r, t = learned.solve_batch(fam, held, q=q, precision=prec, sketches=s_, seed=seed * 30)
+        e1, e3 = learned.gain_errors(r, ref)
+        out[name] = {"solve_s": round(t, 2), "gain1_err_median": float(np.median(e1)), "gain1_err_max": float(e1.max()),
+                     "gain_j<=3_err_median": float(np.median(e3)), "within_1e-3": int((e3 <= 1e-3).sum())}
+    return out
+
+
 def run_reference(args):
     """CPU arm: the reference algorithm on the host cores (oracle port)."""
     rank = int(os.environ.get("RANK", "0"))
@@ -476,6 +519,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batching-form comparison")
     ap.add_argument("--no-gl1", action="store_true", help="skip the 500-node Ginzburg-Landau runs")
     ap.add_argument("--learned", action="store_true", help="run the learned-sketch experiment (about a minute)")
+    ap.add_argument("--learned3d", action="store_true", help="run the 3D learned-sketch experiment (a few minutes)")
     ap.add_argument("--ttg-n", type=int, default=64, help="grid of the time-to-gains solves")
     ap.add_argument("--large-n", type=int, default=0,
                     help="run the precision form on the n^3 operator in capacity mode (128: the 10.5M-row case)")
@@ -580,6 +624,9 @@ def main():
     learned_res = None
     if rank == 0 and args.learned:
         learned_res = learned_form()
+    learned3d = None
+    if rank == 0 and args.learned3d:
+        learned3d = learned3d_form()
     gl1 = None
     if rank == 0 and not args.no_gl1:
         gl1 = gl1_form(min(os.cpu_count() or 1, 10))
@@ -639,6 +686,7 @@ def main():
             "time_to_gains": ttg,
             "batching": batching,
             "learned_sketch": learned_res,
+            "learned_sketch_3d": learned3d,
             "gl1": gl1,
             "precision_form_large": large,
         }

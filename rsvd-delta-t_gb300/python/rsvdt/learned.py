@@ -19,9 +19,14 @@ action on the computed forcing modes checks the gains (| |R v_j| - s_j | /
 s_j for the leading modes); above the threshold the problem is re-solved
 from a random sketch with one power iteration.
 
-Problem family: Ginzburg-Landau operators with the grid spacing of the
+Problem families: Ginzburg-Landau operators with the grid spacing of the
 500-node case (synth.gl_stretched), parameters mu0 in [0.2, 0.45] and the
-advection speed U = Re(nu) in [1.5, 2.5], discounted where unstable.
+advection speed U = Re(nu) in [1.5, 2.5], discounted where unstable
+(Family); and the five-field 3D operator at 48^3 (synth.op3d_blocks) over
+the Reynolds number Re in [500, 2000] and a uniform reaction term mu0 in
+[0.2, 0.45] added to the diagonal, as mu0 enters the Ginzburg-Landau
+operator (Family3D). Each family supplies its points, its network inputs
+(three values in [-1, 1]) and a context with its operator.
 """
 from __future__ import annotations
 
@@ -71,24 +76,148 @@ class Family:
         return rsvdt.default_params(k=self.k, q=q, Nw=self.Nw, w=self.w0, dt=self.dt, TransientLength=self.T,
                                     DiscFlg=int(beta > 0), beta=beta, precision=precision, Display=0)
 
+    batched = True
 
-def solve_batch(fam: Family, pts, q: int, precision: int, sketches=None, seed: int = 0):
-    """RSVD-Delta-t for every point as one batch; returns ([(U, V, S)], seconds).
-    Random sketches (seeded, CN(0,1)) unless `sketches` are given."""
+    def inputs(self, pts) -> np.ndarray:
+        """(mu0, U, w) scaled to [-1, 1], one row per (point, frequency)."""
+        om = self.omegas()
+        rows = []
+        for mu0, U in pts:
+            for w in om:
+                rows.append([2 * (mu0 - self.mu0[0]) / (self.mu0[1] - self.mu0[0]) - 1,
+                             2 * (U - self.U[0]) / (self.U[1] - self.U[0]) - 1,
+                             w / (self.w0 * self.Nw / 2)])
+        return np.asarray(rows, dtype=np.float32)
+
+    def context(self, rsvdt, pt, q: int, precision: int):
+        A, beta = self.operator(pt)
+        ctx = rsvdt.Context(self.params(rsvdt, q, beta, precision))
+        ctx.set_operator(A)
+        return ctx
+
+
+@dataclass
+class Family3D:
+    """The 3D five-field operator at n^3 (N = 5 n^3) over Re and a uniform
+    reaction term mu0: A(Re, mu0) = stencil(Re) + coupling + (mu0 - s) I,
+    with s fixed for the family so that the least stable corner (Re = 2000,
+    mu0 = 0.45) has its rightmost eigenvalue at `target` (estimated with the
+    unforced RK4 propagator, workloads.rk4_growth_rate); every other member
+    is more damped. One time grid for the family: dt from the Gershgorin
+    bound of the stiffest member (Re = 500)."""
+    n: int = 48
+    k: int = 4
+    Nw: int = 16
+    w0: float = 0.1
+    Re: tuple = (500.0, 2000.0)
+    mu0: tuple = (0.2, 0.45)
+    seed: int = 7
+    target: float = -0.05
+    periods: float = 2.0
+
+    batched = False
+
+    def __post_init__(self):
+        self._shift = None
+        self._dt = None
+
+    @property
+    def N(self):
+        return 5 * self.n ** 3
+
+    @property
+    def T(self):
+        return 2 * np.pi / self.w0
+
+    def _setup(self):
+        if self._shift is not None:
+            return
+        from . import workloads
+
+        br, bc, bl = synth.op3d_blocks(n=self.n, Re=self.Re[0], seed=self.seed, shift=-self.mu0[0])
+        rho = workloads.gershgorin_bound_bcsr(br, bc, bl)
+        dt = 2.5 / (rho + 1.0)  # room for the family's shift
+        corner = synth.op3d_blocks(n=self.n, Re=self.Re[1], seed=self.seed, shift=-self.mu0[1])
+        rate, _ = workloads.rk4_growth_rate(corner, self.w0, self.Nw, dt)
+        self._shift = rate - self.target
+        self._dt = dt
+
+    @property
+    def dt(self):
+        self._setup()
+        return self._dt
+
+    @property
+    def shift(self):
+        self._setup()
+        return self._shift
+
+    def omegas(self):
+        return np.array([(i if i <= self.Nw // 2 - 1 else i - self.Nw) * self.w0 for i in range(self.Nw)])
+
+    def points(self, count: int, seed: int):
+        rng = np.random.default_rng(seed)
+        return [(float(rng.uniform(*self.Re)), float(rng.uniform(*self.mu0))) for _ in range(count)]
+
+    def operator(self, pt):
+        Re, mu0 = pt
+        return synth.op3d_blocks(n=self.n, Re=Re, seed=self.seed, shift=self.shift - mu0), 0.0
+
+    def params(self, rsvdt, q: int, beta: float, precision: int):
+        return rsvdt.default_params(k=self.k, q=q, Nw=self.Nw, w=self.w0, dt=self.dt,
+                                    TransientLength=self.periods * self.T, precision=precision, Display=0)
+
+    def inputs(self, pts) -> np.ndarray:
+        """(Re, mu0, w) scaled to [-1, 1] (Re on a log scale)."""
+        om = self.omegas()
+        lo, hi = np.log(self.Re[0]), np.log(self.Re[1])
+        rows = []
+        for Re, mu0 in pts:
+            for w in om:
+                rows.append([2 * (np.log(Re) - lo) / (hi - lo) - 1,
+                             2 * (mu0 - self.mu0[0]) / (self.mu0[1] - self.mu0[0]) - 1,
+                             w / (self.w0 * self.Nw / 2)])
+        return np.asarray(rows, dtype=np.float32)
+
+    def context(self, rsvdt, pt, q: int, precision: int):
+        bcsr, _ = self.operator(pt)
+        ctx = rsvdt.Context(self.params(rsvdt, q, 0.0, precision))
+        ctx.set_operator_bcsr(*bcsr)
+        return ctx
+
+
+def solve_batch(fam, pts, q: int, precision: int, sketches=None, seed: int = 0):
+    """RSVD-Delta-t for every point (one batch for a batched family, one
+    context after another otherwise); returns ([(U, V, S)], seconds of the
+    solves). Random sketches (seeded, CN(0,1)) unless `sketches` are given."""
     import rsvdt
 
-    b = rsvdt.Batch(precision)
-    for pt in pts:
-        A, beta = fam.operator(pt)
-        b.add(fam.params(rsvdt, q, beta, precision), A)
-    for i in range(len(pts)):
-        F = sketches[i] if sketches is not None else synth.complex_normal(fam.N, fam.k * fam.Nw, seed + i)
-        b.set_sketch(i, F)
-    t0 = time.perf_counter()
-    b.run()
-    out = [b.get_results(i) for i in range(len(pts))]
-    dt = time.perf_counter() - t0
-    b.close()
+    def sketch(i):
+        return sketches[i] if sketches is not None else synth.complex_normal(fam.N, fam.k * fam.Nw, seed + i)
+
+    if fam.batched:
+        b = rsvdt.Batch(precision)
+        for pt in pts:
+            A, beta = fam.operator(pt)
+            b.add(fam.params(rsvdt, q, beta, precision), A)
+        for i in range(len(pts)):
+            b.set_sketch(i, sketch(i))
+        t0 = time.perf_counter()
+        b.run()
+        out = [b.get_results(i) for i in range(len(pts))]
+        dt = time.perf_counter() - t0
+        b.close()
+        return out, dt
+    out, dt = [], 0.0
+    for i, pt in enumerate(pts):
+        ctx = fam.context(rsvdt, pt, q, precision)
+        ctx.set_sketch(sketch(i))
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.run()
+        out.append(ctx.get_results())
+        dt += time.perf_counter() - t0
+        ctx.close()
     return out, dt
 
 
@@ -97,6 +226,22 @@ def _phase_fix(C: np.ndarray) -> np.ndarray:
     idx = np.argmax(np.abs(C), axis=0)
     ph = C[idx, np.arange(C.shape[1])]
     return C * (np.abs(ph) / np.where(ph == 0, 1, ph))[None, :]
+
+
+def pod_basis(M: np.ndarray, r: int):
+    """Leading r left singular vectors of M (N x m) and the fraction of
+    |M|_F^2 they hold: from the N x N correlation when N <= m, otherwise by
+    the method of snapshots (Phi = M W Lambda^{-1/2} from M^H M = W Lambda W^H),
+    whose cost does not grow with N^2."""
+    if M.shape[0] <= M.shape[1]:
+        ev, vec = np.linalg.eigh(M @ M.conj().T)
+        ev = ev[::-1]
+        Phi = np.ascontiguousarray(vec[:, ::-1][:, :r])
+    else:
+        ev, W = np.linalg.eigh(M.conj().T @ M)
+        ev, W = ev[::-1], W[:, ::-1]
+        Phi = np.ascontiguousarray((M @ W[:, :r]) / np.sqrt(np.maximum(ev[:r], 1e-300)))
+    return Phi, float(ev[:r].sum() / ev.sum())
 
 
 class LearnedSketch:
@@ -109,15 +254,7 @@ class LearnedSketch:
         self.Phi = None
 
     def _inputs(self, pts):
-        f = self.fam
-        om = f.omegas()
-        rows = []
-        for mu0, U in pts:
-            for w in om:
-                rows.append([2 * (mu0 - f.mu0[0]) / (f.mu0[1] - f.mu0[0]) - 1,
-                             2 * (U - f.U[0]) / (f.U[1] - f.U[0]) - 1,
-                             w / (f.w0 * f.Nw / 2)])
-        return np.asarray(rows, dtype=np.float32)
+        return self.fam.inputs(pts)
 
     def fit(self, pts, modes, steps: int = 3000, batch: int = 256, lr: float = 1e-3):
         """modes: list of V (N x k*Nw, frequency-major) at the points."""
@@ -125,10 +262,7 @@ class LearnedSketch:
 
         f = self.fam
         M = np.concatenate([V for V in modes], axis=1)  # N x (points * k * Nw)
-        G = M @ M.conj().T
-        ev, vec = np.linalg.eigh(G)
-        self.Phi = np.ascontiguousarray(vec[:, ::-1][:, :self.r])
-        self.pod_energy = float(ev[::-1][:self.r].sum() / ev.sum())
+        self.Phi, self.pod_energy = pod_basis(M, self.r)
         T = []
         for V in modes:
             for iw in range(f.Nw):
@@ -162,9 +296,7 @@ def gain_check(fam: Family, pt, result, jmax: int = 3):
     import rsvdt
 
     U, V, S = result
-    A, beta = fam.operator(pt)
-    ctx = rsvdt.Context(fam.params(rsvdt, 0, beta, rsvdt.PREC_C128))
-    ctx.set_operator(A)
+    ctx = fam.context(rsvdt, pt, 0, rsvdt.PREC_C128)
     ctx.set_sketch(V)
     ctx.action(rsvdt.DIRECT)
     Y = ctx.get_block()

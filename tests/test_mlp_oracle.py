@@ -32,3 +32,24 @@ def test_bf16_rounding_is_round_to_nearest_even():
     assert r[2] == np.float32(1.0078125)
     assert r[3] == -2.5
     assert abs(r[4] - 3.0e-3) / 3.0e-3 < 2 ** -8
+
+
+def test_pod_basis_snapshot_method_matches_correlation():
+    """The learned sketch's POD basis: the method of snapshots (tall mode
+    matrices, the 3D family) spans the same leading subspace as the N x N
+    correlation eigenvectors."""
+    from rsvdt import learned
+
+    rng = np.random.default_rng(3)
+    N, m, r = 300, 40, 6
+    base = rng.standard_normal((N, r)) + 1j * rng.standard_normal((N, r))
+    M = base @ (rng.standard_normal((r, m)) * np.logspace(0, -2, r)[:, None]) + 1e-6 * rng.standard_normal((N, m))
+    P1, e1 = learned.pod_basis(M, r)  # snapshots (N > m)
+    ev, vec = np.linalg.eigh(M @ M.conj().T)
+    P2 = vec[:, ::-1][:, :r]
+    assert np.allclose(P1.conj().T @ P1, np.eye(r), atol=1e-10)
+    # Same subspace: the projector difference is at rounding level.
+    assert np.linalg.norm(P1 @ P1.conj().T - P2 @ P2.conj().T) < 1e-8
+    assert abs(e1 - ev[::-1][:r].sum() / ev.sum()) < 1e-12
+    Ps, es = learned.pod_basis(M[:30].copy(), 5)  # wide (N <= m) branch
+    assert np.allclose(Ps.conj().T @ Ps, np.eye(5), atol=1e-10) and 0 < es <= 1
