@@ -758,14 +758,20 @@ rsvdt_status rsvdt_set_operator_bcsr(rsvdt_ctx *ctx, int64_t nb, int32_t bs, con
     d.browptr = (int32_t *)dalloc(ctx, sizeof(int32_t) * (nb + 1));
     d.bcol = (int32_t *)dalloc(ctx, sizeof(int32_t) * (nblk ? nblk : 1));
     d.val = (z128 *)dalloc(ctx, sizeof(z128) * (nblk ? nblk * bb : 1));
-    d.val32 = (z64 *)dalloc(ctx, sizeof(z64) * (nblk ? nblk * bb : 1));
+    const int64_t s32 = bs == 5 ? 26 : bb;
+    d.stride32 = (int32_t)s32;
+    d.val32 = (z64 *)dalloc(ctx, sizeof(z64) * (nblk ? nblk * s32 : 1));
     if (!d.browptr || !d.bcol || !d.val || !d.val32) return set_err(ctx, RSVDT_ERR_OOM, "block-CSR allocation failed");
-    std::vector<z64> v32(v.size());
-    for (size_t e = 0; e < v.size(); ++e) v32[e] = zmake<z64>((float)v[e].real(), (float)v[e].imag());
+    std::vector<z64> v32((size_t)(nblk * s32), zmake<z64>(0.f, 0.f));
+    for (int64_t j = 0; j < nblk; ++j)
+      for (int64_t e = 0; e < bb; ++e) {
+        const std::complex<double> x = v[(size_t)(j * bb + e)];
+        v32[(size_t)(j * s32 + e)] = zmake<z64>((float)x.real(), (float)x.imag());
+      }
     if (!upload(ctx, d.browptr, r.data(), sizeof(int32_t) * (nb + 1)) ||
         (nblk && !upload(ctx, d.bcol, c.data(), sizeof(int32_t) * nblk)) ||
         (nblk && !upload(ctx, d.val, v.data(), sizeof(z128) * nblk * bb)) ||
-        (nblk && !upload(ctx, d.val32, v32.data(), sizeof(z64) * nblk * bb)))
+        (nblk && !upload(ctx, d.val32, v32.data(), sizeof(z64) * nblk * s32)))
       return RSVDT_ERR_CUDA;
     d.present = true;
     return RSVDT_OK;

@@ -105,6 +105,9 @@ struct DevBCSR {
   int32_t *bcol = nullptr;
   z128 *val = nullptr;
   z64 *val32 = nullptr;
+  // Complex64 values per block in val32: bs*bs, padded to 26 for 5x5
+  // blocks so that every block starts on a 16-byte boundary.
+  int32_t stride32 = 0;
 };
 
 }  // namespace rsvdt

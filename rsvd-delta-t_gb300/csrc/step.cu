@@ -53,6 +53,7 @@ struct StepArgs {
   const int32_t *__restrict__ col;
   const Z *__restrict__ val;
   int bs;                     // 0: CSR; >0: block CSR with bs x bs blocks
+  int bstride;                // values per block in `val` (bs*bs; 26 for 5x5 complex64)
   const Z *__restrict__ Fh;   // [slab][n][k], nullptr when unforced
   const Z *__restrict__ tab;  // [2Ns][Nw]
   Z *y, *zA, *zB, *acc, *F2, *F3, *ring;
@@ -189,7 +190,7 @@ __device__ __forceinline__ void row_product(const StepArgs<Z> &P, int64_t n, int
     int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
     for (int32_t j = b; j < e; ++j) {
       const int64_t c0 = (int64_t)__ldg(P.col + j) * bs;
-      const Z *blkrow = P.val + ((int64_t)j * bs + r) * bs;
+      const Z *blkrow = P.val + (int64_t)j * P.bstride + r * bs;
       for (int c = 0; c < bs; ++c) {
         const Z a = blkrow[c];
         const Z v = x[(c0 + c) * K + kc];
@@ -295,8 +296,12 @@ static const int kRowThreads = 128;
 // packed 32/L to a warp. Vector rows (y, acc, the forcing slabs, ...) are
 // read and written the same way: the lanes of consecutive block rows cover
 // consecutive bytes.
+// Stages 2-4 are held to 64 registers (8 blocks per SM): more warps in
+// flight for their latency-bound gathers (measured faster on the 64^3
+// operator than the unbounded 108-register build); stage 1 keeps its
+// registers for the forcing synthesis.
 template <class Z, int K, int KP, int S>
-__global__ void __launch_bounds__(kRowThreads) k_bstage(const StepArgs<Z> P) {
+__global__ void __launch_bounds__(kRowThreads, S == 1 ? 1 : 8) k_bstage(const StepArgs<Z> P) {
   constexpr int L = K / KP;
   constexpr int BPW = 32 / L;
   extern __shared__ unsigned char smem_raw[];
@@ -335,16 +340,37 @@ __global__ void __launch_bounds__(kRowThreads) k_bstage(const StepArgs<Z> P) {
     const int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
     for (int32_t j = b; j < e; ++j) {
       const int64_t c0 = (int64_t)__ldg(P.col + j) * 5;
-      const Z *blk = P.val + (int64_t)j * 25;
+      const Z *blk = P.val + (int64_t)j * P.bstride;
+      if constexpr (S == 4 && sizeof(Z) == 8) {
+        // The padded 26-value block as 13 aligned 16-byte loads.
+        Z a[26];
+        const float4 *b4 = reinterpret_cast<const float4 *>(blk);
 #pragma unroll
-      for (int c = 0; c < 5; ++c) {
-        Z xv[KP];
-        ldg_chunk<Z, KP>(x + (c0 + c) * K + q * KP, xv);
+        for (int m = 0; m < 13; ++m) {
+          const float4 t = __ldg(b4 + m);
+          a[2 * m] = zmake<Z>(t.x, t.y);
+          a[2 * m + 1] = zmake<Z>(t.z, t.w);
+        }
 #pragma unroll
-        for (int r = 0; r < 5; ++r) {
-          const Z a = blk[r * 5 + c];
+        for (int c = 0; c < 5; ++c) {
+          Z xv[KP];
+          ldg_chunk<Z, KP>(x + (c0 + c) * K + q * KP, xv);
 #pragma unroll
-          for (int p = 0; p < KP; ++p) zmac(k[r][p], a, xv[p]);
+          for (int r = 0; r < 5; ++r)
+#pragma unroll
+            for (int p = 0; p < KP; ++p) zmac(k[r][p], a[r * 5 + c], xv[p]);
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+          Z xv[KP];
+          ldg_chunk<Z, KP>(x + (c0 + c) * K + q * KP, xv);
+#pragma unroll
+          for (int r = 0; r < 5; ++r) {
+            const Z a = blk[r * 5 + c];
+#pragma unroll
+            for (int p = 0; p < KP; ++p) zmac(k[r][p], a, xv[p]);
+          }
         }
       }
     }
@@ -597,7 +623,7 @@ __global__ void __launch_bounds__(kRowThreads) k_rstage(const StepArgs<Z> P) {
     const int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
     for (int32_t j = b; j < e; ++j) {
       const int64_t c0 = (int64_t)__ldg(P.col + j) * 5;
-      const Z *arow = P.val + ((int64_t)j * 5 + r) * 5;
+      const Z *arow = P.val + (int64_t)j * P.bstride + r * 5;
       Z a[5];
 #pragma unroll
       for (int c = 0; c < 5; ++c) a[c] = arow[c];
@@ -720,12 +746,14 @@ static StepArgs<Z> make_args(rsvdt_ctx *ctx, int dir, bool forced) {
     P.col = M.bcol;
     P.val = (const Z *)(c64 ? (void *)M.val32 : (void *)M.val);
     P.bs = M.bs;
+    P.bstride = c64 ? M.stride32 : M.bs * M.bs;
   } else {
     const DevCSR &M = dir ? ctx->A : ctx->AH;
     P.rowptr = M.rowptr;
     P.col = M.col;
     P.val = (const Z *)(c64 ? (void *)M.val32 : (void *)M.val);
     P.bs = 0;
+    P.bstride = 0;
   }
   P.Fh = forced ? (const Z *)ctx->Fh : nullptr;
   P.tab = (const Z *)(c64 ? (void *)ctx->tab32 : (void *)ctx->tab);
@@ -879,14 +907,13 @@ static rsvdt_status run_steps_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t nst
 // batch of one, whose FS lanes split a row's nonzeros and forcing slabs.
 // A small problem (few rows x test vectors, e.g. the 500-node
 // Ginzburg-Landau case) is bound by the dependent-load chain of one
-// thread's forcing synthesis, which the split shortens FS times; the lanes
-// are chosen so that rows x test vectors x FS is about 2^17 threads.
+// thread's forcing synthesis, which the split shortens FS times.
 int step_lanes(const rsvdt_ctx *ctx) {
   if (ctx->lanes_override > 0) return ctx->lanes_override;
-  const int64_t nk = ctx->N * ctx->Ks;
-  int fs = 1;
-  while (fs < 8 && nk * fs * 2 <= ((int64_t)1 << 17)) fs *= 2;
-  return fs;
+  // Measured on GB300: 8 lanes take the 500-node Ginzburg-Landau step (5000
+  // rows x test vectors) from 32 to 27 us; problems a few times larger are
+  // faster with one lane per row.
+  return ctx->N * ctx->Ks <= 8192 ? 8 : 1;
 }
 
 static const int kSmallThreads = 128;
@@ -1156,7 +1183,7 @@ __device__ __forceinline__ void row_product_split(const StepArgs<Z> &P, int64_t 
     const int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
     for (int32_t j = b + fsub; j < e; j += FS) {
       const int64_t c0 = (int64_t)__ldg(P.col + j) * bs;
-      const Z *blkrow = P.val + ((int64_t)j * bs + r) * bs;
+      const Z *blkrow = P.val + (int64_t)j * P.bstride + r * bs;
       for (int c = 0; c < bs; ++c) zmac(acc, blkrow[c], x[(c0 + c) * K + kc]);
     }
   }

@@ -6,7 +6,8 @@ are needed.
 Pipeline (everything heavy runs on the GPU through the C ABI):
   1. the method itself (batched RSVD-Delta-t) computes the top-k forcing
      modes V(p, w) at seeded training points p of a problem family;
-  2. a POD basis Phi (N x r) of all those modes;
+  2. a POD basis Phi (N x r) of all those modes (one basis per frequency
+     for the 3D family, by the method of snapshots);
   3. each mode block projected on Phi, C = Phi^H V (r x k), column phases
      fixed (largest coefficient real and positive), real and imaginary parts
      standardised;
@@ -116,6 +117,7 @@ class Family3D:
     periods: float = 2.0
 
     batched = False
+    pod_per_frequency = True
 
     def __post_init__(self):
         self._shift = None
@@ -252,21 +254,40 @@ class LearnedSketch:
         self.seed = seed
         self.net = None
         self.Phi = None
+        self.per_frequency = False
 
     def _inputs(self, pts):
         return self.fam.inputs(pts)
 
+    def _basis(self, iw):
+        return self.Phi[iw] if self.per_frequency else self.Phi
+
     def fit(self, pts, modes, steps: int = 3000, batch: int = 256, lr: float = 1e-3):
-        """modes: list of V (N x k*Nw, frequency-major) at the points."""
+        """modes: list of V (N x k*Nw, frequency-major) at the points. One
+        POD basis for all frequencies, or one per frequency when the family
+        asks for it (3D modes differ too much between frequencies for one
+        r = 64 basis)."""
         import rsvdt
 
         f = self.fam
-        M = np.concatenate([V for V in modes], axis=1)  # N x (points * k * Nw)
-        self.Phi, self.pod_energy = pod_basis(M, self.r)
+        self.per_frequency = bool(getattr(f, "pod_per_frequency", False))
+        if self.per_frequency:
+            self.Phi, energies = [], []
+            for iw in range(f.Nw):
+                Mw = np.concatenate([V[:, iw * f.k:(iw + 1) * f.k] for V in modes], axis=1)
+                P, e = pod_basis(Mw, min(self.r, Mw.shape[1]))
+                if P.shape[1] < self.r:  # fewer modes than r: pad with zero columns
+                    P = np.concatenate([P, np.zeros((P.shape[0], self.r - P.shape[1]), P.dtype)], axis=1)
+                self.Phi.append(P)
+                energies.append(e)
+            self.pod_energy = float(np.mean(energies))
+        else:
+            M = np.concatenate([V for V in modes], axis=1)  # N x (points * k * Nw)
+            self.Phi, self.pod_energy = pod_basis(M, self.r)
         T = []
         for V in modes:
             for iw in range(f.Nw):
-                C = _phase_fix(self.Phi.conj().T @ V[:, iw * f.k:(iw + 1) * f.k])
+                C = _phase_fix(self._basis(iw).conj().T @ V[:, iw * f.k:(iw + 1) * f.k])
                 T.append(np.concatenate([C.real.ravel(), C.imag.ravel()]))
         T = np.asarray(T, dtype=np.float64)
         self.t_mean = T.mean(axis=0)
@@ -286,7 +307,7 @@ class LearnedSketch:
         rk = self.r * f.k
         for iw in range(f.Nw):
             C = (Y[iw, :rk] + 1j * Y[iw, rk:]).reshape(self.r, f.k)
-            F[:, iw * f.k:(iw + 1) * f.k] = self.Phi @ C
+            F[:, iw * f.k:(iw + 1) * f.k] = self._basis(iw) @ C
         return F
 
 
