@@ -78,3 +78,31 @@ def test_invalid_params_are_rejected_before_the_device(built_lib):
         with pytest.raises(rsvdt.RsvdtError) as e:
             rsvdt.Context(rsvdt.default_params(**kw))
         assert e.value.status == rsvdt.ERR_ARG, bad
+
+
+def test_c_and_ctypes_struct_layouts_agree(built_lib, tmp_path):
+    """sizeof and field offsets of every struct in include/rsvdt.h, from a C
+    compiler, equal the ctypes mirrors the binding passes across the ABI."""
+    import ctypes
+    import subprocess
+
+    import rsvdt
+
+    structs = {"rsvdt_params": rsvdt.Params, "rsvdt_grid": rsvdt.Grid, "rsvdt_trans_params": rsvdt.TransParams,
+               "rsvdt_trans_info": rsvdt.TransInfo}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "rsvdt.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
