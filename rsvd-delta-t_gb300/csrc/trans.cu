@@ -260,8 +260,8 @@ rsvdt_status removal_estimate(rsvdt_ctx *ctx, const TransBuffers &tb, int64_t pe
   const int m = (int)Nw - skip, cols = m + 1;
   const size_t colbytes = sizeof(z128) * (size_t)N * cols;
   int G = H;
-  const size_t budget = (size_t)1 << 31;
-  if (colbytes * (size_t)G > budget) G = (int)std::max<size_t>(1, budget / colbytes);
+  const size_t cap_bytes = (size_t)1 << 31;  // at most 2 GiB of synthetic snapshots at a time
+  if (colbytes * (size_t)G > cap_bytes) G = (int)std::max<size_t>(1, cap_bytes / colbytes);
   const int nchunks = (int)((N + kChunkRows - 1) / kChunkRows);
   z128 *B = (z128 *)dalloc(ctx, colbytes * G);
   z128 *dpart = (z128 *)dalloc(ctx, sizeof(z128) * ((size_t)G * nchunks * cols + (size_t)G * cols + (size_t)G * m));

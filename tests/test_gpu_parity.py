@@ -1,7 +1,7 @@
 """GPU parity: the CUDA path (through the C ABI) against the CPU oracle
 (the C restatement of the reference) on the same seeded inputs.
 
-Tolerances (floating point, complex128 plain form): the spec bar is a
+Tolerances (floating point, complex128 plain form): the target is a
 relative gain error <= 1e-9 and subspace angles <= 1e-7 rad against the
 reference's own run; against the restatement, which performs the same
 operations in the same order up to FMA contraction and summation order, the
