@@ -302,6 +302,7 @@ static rsvdt_status ensure_buffers(rsvdt_ctx *ctx, int64_t K) {
   if (ctx->K == K && ctx->Ks == Ks && ctx->y && ctx->blk_elems >= blk_elems && ctx->buf_capacity == ctx->capacity)
     return RSVDT_OK;
   free_graphs(ctx);
+  ++ctx->blk_version;
   void **bufs[] = {&ctx->y, &ctx->zA, &ctx->zB, &ctx->acc, &ctx->F2, &ctx->F3};
   for (auto b : bufs) {
     dfree(ctx, *b);
@@ -414,6 +415,7 @@ static rsvdt_status weight_step(rsvdt_ctx *ctx, const DevCSR &M, int64_t rows_in
     std::swap(ctx->blk, ctx->blk2);
   }
   ctx->blk_rows = M.rows;
+  ++ctx->blk_version;
   return RSVDT_OK;
 }
 
@@ -421,6 +423,17 @@ static rsvdt_status weight_step(rsvdt_ctx *ctx, const DevCSR &M, int64_t rows_in
 // action's precision (TSActionRK4 copies Y_hat to F_hat,
 // SourceCode/TSActionRK4.c:49).
 static rsvdt_status stage_forcing(rsvdt_ctx *ctx, int prec) { return stage_forcing_coeffs(ctx, prec); }
+
+// Stages the forcing slabs unless they already hold the working block's
+// current contents in this precision.
+static rsvdt_status stage_forcing_cached(rsvdt_ctx *ctx, int prec) {
+  if (ctx->staged_version == ctx->blk_version && ctx->staged_prec == prec && ctx->k0 == 0) return RSVDT_OK;
+  RSVDT_TRY(stage_forcing(ctx, prec));
+  ctx->staged_version = ctx->blk_version;
+  ctx->staged_prec = prec;
+  return RSVDT_OK;
+}
+
 
 namespace rsvdt {
 static rsvdt_status cap_action(rsvdt_ctx *ctx, int d);
@@ -850,6 +863,7 @@ rsvdt_status rsvdt_set_sketch(rsvdt_ctx *ctx, const double *F, int64_t ld, int64
     }
     ctx->blk_rows = rows;
     ctx->have_block = true;
+  ++ctx->blk_version;
     ctx->have_results = false;
     return RSVDT_OK;
   }
@@ -864,6 +878,7 @@ rsvdt_status rsvdt_set_sketch(rsvdt_ctx *ctx, const double *F, int64_t ld, int64
   if (st) return st;
   ctx->blk_rows = rows;
   ctx->have_block = true;
+  ++ctx->blk_version;
   ctx->have_results = false;
   return RSVDT_OK;
 }
@@ -873,6 +888,7 @@ rsvdt_status rsvdt_random_sketch(rsvdt_ctx *ctx, uint64_t seed) {
   RSVDT_TRY(launch_random(ctx, ctx->blk, ctx->Nb * ctx->Nw_eff * ctx->K, seed));
   ctx->blk_rows = ctx->Nb;
   ctx->have_block = true;
+  ++ctx->blk_version;
   ctx->have_results = false;
   return cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
 }
@@ -971,6 +987,7 @@ rsvdt_status action_finish(rsvdt_ctx *ctx, int d) {
   }
   std::swap(ctx->blk, ctx->blk2);
   ctx->blk_rows = ctx->N;
+  ++ctx->blk_version;
   return weights_after(ctx, d);
 }
 
@@ -990,6 +1007,7 @@ static rsvdt_status cap_action(rsvdt_ctx *ctx, int d) {
     if (!st) st = ctx->par.TransientRemoval ? transient_removal(ctx, d, prec, ctx->blk) : launch_dft(ctx, prec, ctx->blk);
   }
   ctx->k0 = 0;
+  ++ctx->blk_version;
   RSVDT_TRY(st);
   ctx->blk_rows = ctx->N;
   return weights_after(ctx, d);
@@ -1001,12 +1019,14 @@ extern "C" {
 
 rsvdt_status rsvdt_qr_all_freqs(rsvdt_ctx *ctx) {
   RSVDT_TRY(require_ready(ctx, true));
+  ++ctx->blk_version;
   RSVDT_TRY(cholqr2(ctx, ctx->blk, ctx->blk_rows, ctx->Nw_eff, ctx->K, nullptr));
   return cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
 }
 
 rsvdt_status rsvdt_svd_all_freqs(rsvdt_ctx *ctx, int32_t before_adjoint) {
   RSVDT_TRY(require_ready(ctx, true));
+  ++ctx->blk_version;
   const int64_t rows = ctx->blk_rows, n = rows * ctx->Nw_eff * ctx->K;
   if (ctx->capacity) return cap_svd(ctx, before_adjoint != 0);
   if (before_adjoint) {
@@ -1109,7 +1129,7 @@ rsvdt_status rsvdt_rk4_reset(rsvdt_ctx *ctx, rsvdt_dir dir) {
   if (ctx->blk_rows != ctx->N) return set_err(ctx, RSVDT_ERR_STATE, "working block must have N rows");
   const int prec = ctx->act_prec;
   ctx->Nstore = ctx->par.TransientRemoval ? ctx->Nw + 1 : ctx->Nw;
-  RSVDT_TRY(stage_forcing(ctx, prec));
+  RSVDT_TRY(stage_forcing_cached(ctx, prec));
   RSVDT_TRY(launch_forcing_init(ctx, dir == RSVDT_DIRECT ? 1 : 0, prec));
   return RSVDT_OK;
 }
@@ -1132,39 +1152,35 @@ rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t 
   if (ctx->capacity) return set_err(ctx, RSVDT_ERR_STATE, "rsvdt_rk4_steps is not available in capacity mode");
   if (ctx->blk_rows != ctx->N) return set_err(ctx, RSVDT_ERR_STATE, "working block must have N rows");
   const int prec = ctx->act_prec;
+  if (prec == RSVDT_PREC_C64)
+    return set_err(ctx, RSVDT_ERR_ARG, "rsvdt_rk4_steps reads back complex128 state only");
   const int64_t N = ctx->N, K = ctx->K;
   ctx->Nstore = ctx->par.TransientRemoval ? ctx->Nw + 1 : ctx->Nw;
-  RSVDT_TRY(stage_forcing(ctx, prec));
-  z128 *stage = (z128 *)dalloc(ctx, sizeof(z128) * N * K * 2);
-  if (!stage) return set_err(ctx, RSVDT_ERR_OOM, "staging allocation failed");
-  rsvdt_status st = RSVDT_OK;
-  // Host (N x K column-major) -> device [n][k]; complex64 form rounds.
-  z128 *ytmp = stage + N * K;
-  auto to_dev = [&](const double *h, void *d) -> rsvdt_status {
-    if (!cuda_ok(ctx, cudaMemcpyAsync(stage, h, sizeof(z128) * N * K, cudaMemcpyHostToDevice, ctx->stream), "upload"))
-      return RSVDT_ERR_CUDA;
-    if (prec == RSVDT_PREC_C64) {
-      RSVDT_TRY(launch_colmajor_to_blk(ctx, stage, N, N, K, ytmp));
-      return launch_convert_to64(ctx, ytmp, (z64 *)d, N * K);
-    }
-    return launch_colmajor_to_blk(ctx, stage, N, N, K, (z128 *)d);
-  };
-  st = to_dev(y, ctx->y);
-  if (!st && !cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync")) st = RSVDT_ERR_CUDA;
-  if (!st) st = to_dev(F3, ctx->F3);
-  if (!st) st = run_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, prec, i0, nsteps, true);
-  auto to_host = [&](void *d, double *h) -> rsvdt_status {
-    const z128 *src = (const z128 *)d;
-    if (prec == RSVDT_PREC_C64) return set_err(ctx, RSVDT_ERR_ARG, "rsvdt_rk4_steps reads back complex128 state only");
-    RSVDT_TRY(launch_blk_to_colmajor(ctx, src, N, K, stage, N));
-    if (!cuda_ok(ctx, cudaMemcpyAsync(h, stage, sizeof(z128) * N * K, cudaMemcpyDeviceToHost, ctx->stream), "download"))
-      return RSVDT_ERR_CUDA;
-    return cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
-  };
-  if (!st) st = to_host(ctx->y, y);
-  if (!st) st = to_host(ctx->F3, F3);
-  dfree(ctx, stage);
-  return st;
+  RSVDT_TRY(stage_forcing_cached(ctx, prec));
+  // One persistent staging buffer for both host arrays (no allocation, and
+  // so no device-wide synchronisation of cudaFree, per call).
+  const size_t need = sizeof(z128) * (size_t)N * K * 2;
+  if (ctx->io_bytes < need) {
+    dfree(ctx, ctx->io_stage);
+    ctx->io_stage = (z128 *)dalloc(ctx, need);
+    ctx->io_bytes = ctx->io_stage ? need : 0;
+    if (!ctx->io_stage) return set_err(ctx, RSVDT_ERR_OOM, "staging allocation failed");
+  }
+  z128 *sy = ctx->io_stage, *sf = ctx->io_stage + N * K;
+  const size_t bytes = sizeof(z128) * (size_t)N * K;
+  // Host (N x K column-major) -> device [n][k], both arrays in flight.
+  if (!cuda_ok(ctx, cudaMemcpyAsync(sy, y, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload") ||
+      !cuda_ok(ctx, cudaMemcpyAsync(sf, F3, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload"))
+    return RSVDT_ERR_CUDA;
+  RSVDT_TRY(launch_colmajor_to_blk(ctx, sy, N, N, K, (z128 *)ctx->y));
+  RSVDT_TRY(launch_colmajor_to_blk(ctx, sf, N, N, K, (z128 *)ctx->F3));
+  RSVDT_TRY(run_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, prec, i0, nsteps, true));
+  RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->y, N, K, sy, N));
+  RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->F3, N, K, sf, N));
+  if (!cuda_ok(ctx, cudaMemcpyAsync(y, sy, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download") ||
+      !cuda_ok(ctx, cudaMemcpyAsync(F3, sf, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download"))
+    return RSVDT_ERR_CUDA;
+  return cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
 }
 
 rsvdt_status rsvdt_synchronize(rsvdt_ctx *ctx) {

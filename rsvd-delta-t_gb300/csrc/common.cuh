@@ -166,6 +166,14 @@ struct rsvdt_ctx {
 
   // Precision of the running action (rsvdt_precision's C128 or C64).
   int act_prec = 0;
+  // Version of the working block's contents (bumped by every call that
+  // writes it) and the version / precision the forcing slabs were staged
+  // from, so that repeated rsvdt_rk4_steps calls restage only when needed.
+  uint64_t blk_version = 1, staged_version = 0;
+  int staged_prec = -1;
+  // Persistent host-transfer staging for rsvdt_rk4_steps.
+  rsvdt::z128 *io_stage = nullptr;
+  size_t io_bytes = 0;
   // Test vectors held by the RK4 state, ring and forcing slabs (Ks = K, or
   // the chunk size in capacity mode) and the first of them in the block.
   int64_t Ks = 0, k0 = 0;

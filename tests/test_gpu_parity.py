@@ -103,6 +103,32 @@ def test_rk4_steps_match_oracle(built_lib, direction):
     ctx.close()
 
 
+def test_rk4_steps_continue_and_restage(built_lib):
+    """Two calls of 10 steps equal one call of 20 (the staged forcing is
+    reused between calls), and a new sketch is restaged (results follow
+    the new forcing, against the oracle)."""
+    A, cfg = small_gl()
+    k = 2
+    ctx = make_ctx(A, cfg, k=k)
+    g = ctx.grid()
+    N, nwe = A.shape[0], g.Nw_eff
+    y0 = synth.complex_normal(N, k, 16)
+    F30 = synth.complex_normal(N, k, 17)
+    for seed in (18, 19):
+        F = synth.complex_normal(N, k * nwe, seed)
+        ctx.set_sketch(F)
+        y1, F31 = ctx.rk4_steps(1, 5, 20, y0.copy(), F30.copy())
+        ya, F3a = ctx.rk4_steps(1, 5, 10, y0.copy(), F30.copy())
+        yb, F3b = ctx.rk4_steps(1, 15, 10, ya, F3a)
+        assert np.array_equal(yb, y1) and np.array_equal(F3b, F31)
+        orc = make_oracle(A, cfg)
+        for ik in range(k):
+            Fk = F[:, [iw * k + ik for iw in range(nwe)]]
+            yo, _ = orc.rk4_steps(1, Fk, 5, 20, y0[:, ik], F30[:, ik])
+            assert rel(y1[:, ik], yo) < 1e-11, seed
+    ctx.close()
+
+
 @pytest.mark.parametrize("direction,tr", [(1, False), (0, False), (1, True), (0, True)])
 def test_action_matches_oracle(built_lib, direction, tr):
     """One resolvent action (TSActionRK4 + DFT or transient removal)."""
