@@ -60,6 +60,7 @@ def lib() -> C.CDLL:
                                  C.c_int, C.c_int]
         L.orc_destroy.argtypes = [C.c_void_p]
         L.orc_set_threads.argtypes = [C.c_void_p, C.c_int]
+        L.orc_set_row_threads.argtypes = [C.c_void_p, C.c_int]
         L.orc_set_weight.argtypes = [C.c_void_p, C.c_int, i64, i64, P(i64), P(i64), d]
         L.orc_ts_action.argtypes = [C.c_void_p, C.c_int, i64, d, d]
         L.orc_action.argtypes = [C.c_void_p, C.c_int, i64, d, d]
@@ -128,6 +129,10 @@ class Oracle:
 
     def set_threads(self, n: int):
         lib().orc_set_threads(self._h, n)
+
+    def set_row_threads(self, n: int):
+        """Threads for the row loops of each RK4 step (results unchanged)."""
+        lib().orc_set_row_threads(self._h, n)
 
     def set_weight(self, which: int, M):
         M = M.tocsr()

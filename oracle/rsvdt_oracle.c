@@ -42,6 +42,7 @@ typedef struct {
   int64_t N, Nw, Nw_eff, Ns, Nt, R;
   double w, dt;
   int tr, real_op, nthreads;
+  int row_threads; /* > 1: the RK4 step's row loops run on that many threads */
   csr_t A, AH;
   zc *idft; /* Nw_eff x 2Ns, row-major */
   zc *dft;  /* Nw x Nw_eff, column-major */
@@ -105,6 +106,17 @@ static int csr_conj_transpose(const csr_t *a, csr_t *t) {
 }
 
 /* out = A x + f (MatMultAdd, SourceCode/TSRK4.c:18,31,33,35); f may be NULL. */
+static void spmv_add_rows(const csr_t *a, const zc *x, const zc *f, zc *out, int nth) {
+  /* Rows are independent: the same sums in the same order on any number of
+   * threads. */
+#pragma omp parallel for schedule(static) num_threads(nth > 1 ? nth : 1) if (nth > 1)
+  for (int64_t i = 0; i < a->rows; ++i) {
+    zc s = f ? f[i] : 0.0;
+    for (int64_t j = a->rowptr[i]; j < a->rowptr[i + 1]; ++j) s += a->val[j] * x[a->col[j]];
+    out[i] = s;
+  }
+}
+
 static void spmv_add(const csr_t *a, const zc *x, const zc *f, zc *out) {
   for (int64_t i = 0; i < a->rows; ++i) {
     zc s = f ? f[i] : 0.0;
@@ -229,6 +241,8 @@ void orc_destroy(void *vh) {
 
 void orc_set_threads(void *vh, int nthreads) { ((orc_t *)vh)->nthreads = nthreads; }
 
+void orc_set_row_threads(void *vh, int nthreads) { ((orc_t *)vh)->row_threads = nthreads; }
+
 int orc_set_weight(void *vh, int which, int64_t rows, int64_t cols, const int64_t *rowptr,
                    const int64_t *col, const double *val) {
   orc_t *h = (orc_t *)vh;
@@ -259,15 +273,22 @@ static int work_alloc(work_t *w, int64_t N) {
 }
 
 /* F = Fk * idft[:, jt] (SourceCode/CreateForcingOnFly.c:17-19). Fk is
- * N x Nw_eff column-major. */
+ * N x Nw_eff column-major. Each F[n] sums over the frequencies in order. */
 static void forcing(const orc_t *h, const zc *Fk, int64_t jt, zc *F) {
   int64_t N = h->N, Nt2 = 2 * h->Ns;
-  for (int64_t n = 0; n < N; ++n) F[n] = 0;
-  for (int64_t iw = 0; iw < h->Nw_eff; ++iw) {
-    zc e = h->idft[iw * Nt2 + jt];
-    const zc *c = Fk + iw * N;
-    for (int64_t n = 0; n < N; ++n) F[n] += c[n] * e;
+  const int nth = h->row_threads;
+#pragma omp parallel for schedule(static) num_threads(nth > 1 ? nth : 1) if (nth > 1)
+  for (int64_t n = 0; n < N; ++n) {
+    zc s = 0;
+    for (int64_t iw = 0; iw < h->Nw_eff; ++iw) s += Fk[iw * N + n] * h->idft[iw * Nt2 + jt];
+    F[n] = s;
   }
+}
+
+/* y_out[n] = a * x[n] + y[n] over all rows (VecWAXPY / VecAXPY). */
+static void waxpy_rows(int64_t N, double a, const zc *x, const zc *y, zc *out, int nth) {
+#pragma omp parallel for schedule(static) num_threads(nth > 1 ? nth : 1) if (nth > 1)
+  for (int64_t n = 0; n < N; ++n) out[n] = a * x[n] + y[n];
 }
 
 /* Half-step forcing indices of step i (SourceCode/TSRK4.c:21-26). */
@@ -289,21 +310,22 @@ static void rk4_step(const orc_t *h, int dir, const zc *Fk, int64_t i, zc *y, zc
   const csr_t *A = dir ? &h->A : &h->AH;
   int64_t N = h->N;
   double dt = h->dt;
+  const int nth = h->row_threads;
   int64_t j2, j3;
-  spmv_add(A, y, F3, w->k1);
+  spmv_add_rows(A, y, F3, w->k1, nth);
   step_indices(h, dir, i, &j2, &j3);
   forcing(h, Fk, j2, w->F2);
   forcing(h, Fk, j3, F3);
-  for (int64_t n = 0; n < N; ++n) w->yt[n] = dt / 2 * w->k1[n] + y[n];
-  spmv_add(A, w->yt, w->F2, w->k2);
-  for (int64_t n = 0; n < N; ++n) w->yt[n] = dt / 2 * w->k2[n] + y[n];
-  spmv_add(A, w->yt, w->F2, w->k3);
-  for (int64_t n = 0; n < N; ++n) w->yt[n] = dt * w->k3[n] + y[n];
-  spmv_add(A, w->yt, F3, w->k4);
-  for (int64_t n = 0; n < N; ++n) y[n] += dt / 6 * w->k1[n];
-  for (int64_t n = 0; n < N; ++n) y[n] += dt / 6 * 2 * w->k2[n];
-  for (int64_t n = 0; n < N; ++n) y[n] += dt / 6 * 2 * w->k3[n];
-  for (int64_t n = 0; n < N; ++n) y[n] += dt / 6 * w->k4[n];
+  waxpy_rows(N, dt / 2, w->k1, y, w->yt, nth);
+  spmv_add_rows(A, w->yt, w->F2, w->k2, nth);
+  waxpy_rows(N, dt / 2, w->k2, y, w->yt, nth);
+  spmv_add_rows(A, w->yt, w->F2, w->k3, nth);
+  waxpy_rows(N, dt, w->k3, y, w->yt, nth);
+  spmv_add_rows(A, w->yt, F3, w->k4, nth);
+  waxpy_rows(N, dt / 6, w->k1, y, y, nth);
+  waxpy_rows(N, dt / 6 * 2, w->k2, y, y, nth);
+  waxpy_rows(N, dt / 6 * 2, w->k3, y, y, nth);
+  waxpy_rows(N, dt / 6, w->k4, y, y, nth);
 }
 
 /* Unforced RK4 step (SourceCode/TSTransRK4.c:15-36). */

@@ -43,6 +43,8 @@ void *orc_create(int64_t N, const int64_t *rowptr, const int64_t *col, const dou
 void orc_destroy(void *h);
 /* Number of OpenMP threads used by the time-stepping loops (<=0: all). */
 void orc_set_threads(void *h, int nthreads);
+/* Threads for the row loops of one RK4 step (1: serial). */
+void orc_set_row_threads(void *h, int nthreads);
 
 /* Weight / input / output matrices (SourceCode/ReadWeightMats.c:26-99):
  * which = 0 W_f^{-1/2} (Nb x Nb), 1 B (N x Nb), 2 C (Nc x N),

@@ -162,3 +162,18 @@ def test_oracle_reproduces_the_tutorial_peak():
     Sd = np.array(g["dense_gains"])
     iw = int(np.argmax(Sd[0]))
     assert abs(S[0, iw] - Sd[0, iw]) / Sd[0, iw] < 1e-4
+
+
+def test_row_threads_do_not_change_the_result():
+    """The RK4 step's row loops on several threads (the CPU baseline's
+    setting) give bit-identical results: rows are independent and each sum
+    keeps its order."""
+    A, w, Nw, dt, T = _small()
+    o = oracle.Oracle(A, Nw, w, dt, T)
+    F = synth.complex_normal(64, Nw, 9)
+    y0 = synth.complex_normal(64, 1, 10)[:, 0]
+    f0 = synth.complex_normal(64, 1, 11)[:, 0]
+    ya, fa = o.rk4_steps(1, F, 3, 25, y0.copy(), f0.copy())
+    o.set_row_threads(4)
+    yb, fb = o.rk4_steps(1, F, 3, 25, y0.copy(), f0.copy())
+    assert np.array_equal(ya, yb) and np.array_equal(fa, fb)
