@@ -221,6 +221,16 @@ rsvdt_status rsvdt_get_capacity(const rsvdt_ctx *ctx, int64_t *kc);
 rsvdt_status rsvdt_set_lanes_per_row(rsvdt_ctx *ctx, int32_t lanes);
 int32_t rsvdt_get_lanes_per_row(const rsvdt_ctx *ctx);
 
+/* Wall time per phase since creation (or the last reset) as a JSON object:
+ * actions run per direction, RK4 steps, seconds spent preparing actions
+ * (weights, forcing slabs), stepping, finishing them (DFT or transient
+ * removal, weights), in QR and in SVD, the mean step time, the lanes per
+ * row and the capacity chunk. The reference prints the same phases as
+ * elapsed times (SourceCode/TSActionRK4.c:150-160, DisplayProgress.c);
+ * with Display >= 1 the library prints them too. */
+rsvdt_status rsvdt_get_timings(const rsvdt_ctx *ctx, char *json, int64_t len);
+rsvdt_status rsvdt_reset_timings(rsvdt_ctx *ctx);
+
 /* Free and total memory of the current CUDA device, in bytes (for callers
  * deciding on the capacity mode before they create the buffers). */
 rsvdt_status rsvdt_device_memory(int64_t *free_bytes, int64_t *total_bytes);

@@ -1,5 +1,6 @@
 // C ABI of the GB300 RSVD-Delta-t library (include/rsvdt.h): context,
 // operator/weight upload, the resolvent actions and the main sequence.
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
@@ -437,6 +438,51 @@ static rsvdt_status stage_forcing_cached(rsvdt_ctx *ctx, int prec) {
 
 namespace rsvdt {
 static rsvdt_status cap_action(rsvdt_ctx *ctx, int d);
+}
+
+// ---------------------------------------------------- progress and timing
+
+static double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+static void print_hms(const char *prefix, double sec, const char *suffix) {
+  const int t = (int)sec, hh = t / 3600, mm = (t - 3600 * hh) / 60, ss = t - 3600 * hh - 60 * mm;
+  printf("%s%02d:%02d:%02d%s", prefix, hh, mm, ss, suffix);
+  fflush(stdout);  // as PetscPrintf: visible at once, also through a pipe
+}
+
+// The RK4 steps of an action (all test vectors of the chunk at once), with
+// the progress lines of SourceCode/DisplayProgress.c:18-50: every 10% of
+// the steps at Display = 2 (the stepping then runs in ten pieces, each
+// ended by a synchronisation), the elapsed time at Display >= 1.
+static rsvdt_status steps_with_progress(rsvdt_ctx *ctx, int d, int prec, int64_t rend) {
+  const double t0 = now_s();
+  if (ctx->par.Display >= 2 && rend >= 10) {
+    int64_t done = 0;
+    for (int p = 0; p < 10; ++p) {
+      const int64_t upto = rend * (p + 1) / 10;
+      printf("Progress percentage: %d%%\n", 10 * p);
+      print_hms("Elapsed time = ", now_s() - t0, "\n");
+      RSVDT_TRY(run_steps(ctx, d, prec, 1 + done, upto - done, true));
+      if (!cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync")) return RSVDT_ERR_CUDA;
+      done = upto;
+    }
+    printf("Progress percentage: 100%%\n");
+    fflush(stdout);
+  } else {
+    RSVDT_TRY(run_steps(ctx, d, prec, 1, rend, true));
+    if (!cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync")) return RSVDT_ERR_CUDA;
+  }
+  const double el = now_s() - t0;
+  ctx->tm.stepping += el;
+  ctx->tm.steps += rend;
+  if (ctx->par.Display >= 1) {
+    char tail[96];
+    snprintf(tail, sizeof tail, " (k = %lld out of %lld)\n", (long long)(ctx->k0 + ctx->Ks), (long long)ctx->K);
+    print_hms("Elapsed time = ", el, tail);
+  }
+  return RSVDT_OK;
 }
 
 // ---------------------------------------------------------- capacity mode
@@ -914,11 +960,24 @@ rsvdt_status rsvdt_get_block(rsvdt_ctx *ctx, double *Y, int64_t ld, int64_t *row
 rsvdt_status rsvdt_action(rsvdt_ctx *ctx, rsvdt_dir dir) {
   RSVDT_TRY(require_ready(ctx, true));
   const int d = dir == RSVDT_DIRECT ? 1 : 0;
-  if (ctx->capacity) return cap_action(ctx, d);
-  int64_t rend = 0;
-  RSVDT_TRY(rsvdt::action_prepare(ctx, d, &rend));
-  RSVDT_TRY(run_steps(ctx, d, ctx->act_prec, 1, rend, true));
-  return rsvdt::action_finish(ctx, d);
+  const double t0 = now_s();
+  ctx->tm.actions[d] += 1;
+  rsvdt_status st;
+  if (ctx->capacity) {
+    st = cap_action(ctx, d);
+  } else {
+    int64_t rend = 0;
+    RSVDT_TRY(rsvdt::action_prepare(ctx, d, &rend));
+    if (!cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync")) return RSVDT_ERR_CUDA;
+    ctx->tm.prepare += now_s() - t0;
+    RSVDT_TRY(steps_with_progress(ctx, d, ctx->act_prec, rend));
+    const double t1 = now_s();
+    st = rsvdt::action_finish(ctx, d);
+    ctx->tm.finish += now_s() - t1;
+  }
+  if (st == RSVDT_OK && ctx->par.Display >= 1)
+    print_hms(d ? "*** Direct action elapsed time = " : "*** Adjoint action elapsed time = ", now_s() - t0, " ***\n");
+  return st;
 }
 
 }  // extern "C"
@@ -936,7 +995,10 @@ static rsvdt_status weights_before(rsvdt_ctx *ctx, int d, int64_t *rend_out) {
   if (ctx->blk_rows != rows_in)
     return set_err(ctx, RSVDT_ERR_STATE, "%s action needs a block of %lld rows, the working block has %lld",
                    d ? "direct" : "adjoint", (long long)rows_in, (long long)ctx->blk_rows);
-  if (ctx->par.Display >= 1) printf("\n*** %s action begins! ***\n", d ? "Direct" : "Adjoint");
+  if (ctx->par.Display >= 1) {
+    printf("\n*** %s action begins! ***\n", d ? "Direct" : "Adjoint");
+    fflush(stdout);
+  }
   if (d) {
     RSVDT_TRY(weight_step(ctx, ctx->W[RSVDT_W_F_SQRT_INV], ctx->blk_rows));
     RSVDT_TRY(weight_step(ctx, ctx->W[RSVDT_B], ctx->blk_rows));
@@ -965,7 +1027,10 @@ static rsvdt_status weights_after(rsvdt_ctx *ctx, int d) {
   bool ok = true;
   RSVDT_TRY(check_finite(ctx, ctx->blk, ctx->blk_rows * ctx->Nw_eff * ctx->K, &ok));
   if (!ok) return set_err(ctx, RSVDT_ERR_DIVERGED, "NaN or Inf in the %s action's response", d ? "direct" : "adjoint");
-  if (ctx->par.Display >= 1) printf("*** %s action done ***\n", d ? "Direct" : "Adjoint");
+  if (ctx->par.Display >= 1) {
+    printf("*** %s action done ***\n", d ? "Direct" : "Adjoint");
+    fflush(stdout);
+  }
   return RSVDT_OK;
 }
 
@@ -1003,7 +1068,7 @@ static rsvdt_status cap_action(rsvdt_ctx *ctx, int d) {
     ctx->k0 = k0;
     st = stage_forcing(ctx, prec);
     if (!st) st = launch_forcing_init(ctx, d, prec);
-    if (!st) st = run_steps(ctx, d, prec, 1, rend, true);
+    if (!st) st = steps_with_progress(ctx, d, prec, rend);
     if (!st) st = ctx->par.TransientRemoval ? transient_removal(ctx, d, prec, ctx->blk) : launch_dft(ctx, prec, ctx->blk);
   }
   ctx->k0 = 0;
@@ -1020,11 +1085,23 @@ extern "C" {
 rsvdt_status rsvdt_qr_all_freqs(rsvdt_ctx *ctx) {
   RSVDT_TRY(require_ready(ctx, true));
   ++ctx->blk_version;
+  const double t0 = now_s();
   RSVDT_TRY(cholqr2(ctx, ctx->blk, ctx->blk_rows, ctx->Nw_eff, ctx->K, nullptr));
-  return cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
+  if (!cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync")) return RSVDT_ERR_CUDA;
+  ctx->tm.qr += now_s() - t0;
+  return RSVDT_OK;
 }
 
+static rsvdt_status svd_all_freqs_impl(rsvdt_ctx *ctx, int32_t before_adjoint);
+
 rsvdt_status rsvdt_svd_all_freqs(rsvdt_ctx *ctx, int32_t before_adjoint) {
+  const double t0 = now_s();
+  const rsvdt_status st = svd_all_freqs_impl(ctx, before_adjoint);
+  if (ctx) ctx->tm.svd += now_s() - t0;
+  return st;
+}
+
+static rsvdt_status svd_all_freqs_impl(rsvdt_ctx *ctx, int32_t before_adjoint) {
   RSVDT_TRY(require_ready(ctx, true));
   ++ctx->blk_version;
   const int64_t rows = ctx->blk_rows, n = rows * ctx->Nw_eff * ctx->K;
@@ -1204,6 +1281,25 @@ rsvdt_status rsvdt_set_capacity_mode(rsvdt_ctx *ctx, int64_t kc, int32_t u_c64) 
     update_dims(ctx);
     RSVDT_TRY(ensure_buffers(ctx, ctx->K > 0 ? ctx->K : ctx->par.k));
   }
+  return RSVDT_OK;
+}
+
+rsvdt_status rsvdt_get_timings(const rsvdt_ctx *ctx, char *json, int64_t len) {
+  if (!ctx || !json || len < 1) return RSVDT_ERR_ARG;
+  const auto &t = ctx->tm;
+  const double ms = t.steps ? 1e3 * t.stepping / (double)t.steps : 0.0;
+  const int n = snprintf(json, (size_t)len,
+                         "{\"actions\": {\"direct\": %lld, \"adjoint\": %lld}, \"steps\": %lld, "
+                         "\"seconds\": {\"prepare\": %.6f, \"stepping\": %.6f, \"finish\": %.6f, \"qr\": %.6f, "
+                         "\"svd\": %.6f}, \"ms_per_step\": %.6f, \"lanes_per_row\": %d, \"capacity_chunk\": %lld}",
+                         (long long)t.actions[1], (long long)t.actions[0], (long long)t.steps, t.prepare, t.stepping,
+                         t.finish, t.qr, t.svd, ms, step_lanes(ctx), (long long)(ctx->capacity ? ctx->Ks : 0));
+  return n < len ? RSVDT_OK : RSVDT_ERR_ARG;
+}
+
+rsvdt_status rsvdt_reset_timings(rsvdt_ctx *ctx) {
+  if (!ctx) return RSVDT_ERR_ARG;
+  ctx->tm = rsvdt_ctx::PhaseTimes();
   return RSVDT_OK;
 }
 

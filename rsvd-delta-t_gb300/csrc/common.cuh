@@ -171,6 +171,12 @@ struct rsvdt_ctx {
   // from, so that repeated rsvdt_rk4_steps calls restage only when needed.
   uint64_t blk_version = 1, staged_version = 0;
   int staged_prec = -1;
+  // Wall time per phase (seconds; phases end at a stream synchronisation)
+  // for rsvdt_get_timings.
+  struct PhaseTimes {
+    double prepare = 0, stepping = 0, finish = 0, qr = 0, svd = 0;
+    int64_t actions[2] = {0, 0}, steps = 0;
+  } tm;
   // Persistent host-transfer staging for rsvdt_rk4_steps.
   rsvdt::z128 *io_stage = nullptr;
   size_t io_bytes = 0;

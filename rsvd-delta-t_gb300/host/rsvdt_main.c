@@ -531,6 +531,10 @@ int main(int argc, char **argv) {
   printf("\n********************************************\n*************** RSVD-\\Delta t **************\n"
          "********************************************\n");
   check(ctx, rsvdt_run(ctx), "RSVD-Delta-t");
+  if (p.Display >= 1) {
+    char js[1024];
+    if (rsvdt_get_timings(ctx, js, sizeof js) == RSVDT_OK) printf("Timings: %s\n", js);
+  }
 
   /* SaveResults (SourceCode/SaveResults.c:32-92), one file's columns at a
    * time (a file is N x Nw_eff or N x k; the whole U and V may not fit in

@@ -40,7 +40,7 @@ EXPORTED = [
     "rsvdt_rk4_profile", "rsvdt_synchronize", "rsvdt_stream", "rsvdt_launch_count",
     "rsvdt_qr_all_freqs_noalloc", "rsvdt_trans_grid", "rsvdt_trans_run",
     "rsvdt_set_capacity_mode", "rsvdt_get_capacity", "rsvdt_get_result_cols", "rsvdt_device_memory",
-    "rsvdt_set_lanes_per_row", "rsvdt_get_lanes_per_row",
+    "rsvdt_set_lanes_per_row", "rsvdt_get_lanes_per_row", "rsvdt_get_timings", "rsvdt_reset_timings",
     "rsvdt_batch_create", "rsvdt_batch_destroy", "rsvdt_batch_last_error", "rsvdt_batch_add",
     "rsvdt_batch_set_sketch", "rsvdt_batch_random_sketch", "rsvdt_batch_run", "rsvdt_batch_get_results",
     "rsvdt_batch_get_grid", "rsvdt_batch_get_tuning", "rsvdt_batch_launch_count",
@@ -148,6 +148,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "rsvdt_set_capacity_mode": (C.c_int, [vp, i64, C.c_int32]),
         "rsvdt_get_capacity": (C.c_int, [vp, P(i64)]),
         "rsvdt_device_memory": (C.c_int, [P(i64), P(i64)]),
+        "rsvdt_get_timings": (C.c_int, [vp, C.c_char_p, i64]),
+        "rsvdt_reset_timings": (C.c_int, [vp]),
         "rsvdt_set_lanes_per_row": (C.c_int, [vp, C.c_int32]),
         "rsvdt_get_lanes_per_row": (C.c_int32, [vp]),
         "rsvdt_get_result_cols": (C.c_int, [vp, P(i64), i64, d, i64, d, i64]),
@@ -357,6 +359,17 @@ class Context:
         self._check(self._lib.rsvdt_rk4_profile(self._h, direction, i0, nsteps,
                                                 out.ctypes.data_as(C.POINTER(C.c_double))))
         return out.tolist()
+
+    def timings(self) -> dict:
+        """Wall time per phase (rsvdt_get_timings) as a dict."""
+        import json
+
+        buf = C.create_string_buffer(1024)
+        self._check(self._lib.rsvdt_get_timings(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
+    def reset_timings(self) -> None:
+        self._check(self._lib.rsvdt_reset_timings(self._h))
 
     def set_lanes_per_row(self, lanes: int) -> None:
         """1: stage kernels with one thread per row; 2/4/8: the batched

@@ -356,6 +356,36 @@ def test_refine_form_recovers_fp64_gains(built_lib):
     assert eref[0].max() < e64[0].max() and eref[:3].max() < 1e-3
 
 
+def test_progress_output_and_phase_timings(built_lib, capfd):
+    """Display = 2 prints the reference's progress lines
+    (SourceCode/DisplayProgress.c:18-50, SourceCode/TSActionRK4.c:150-160);
+    rsvdt_get_timings counts the actions and steps of the run and splits
+    its wall time into phases."""
+    import rsvdt
+    A, cfg = small_gl()
+    k = 2
+    p = rsvdt.default_params(k=k, q=1, Nw=cfg["Nw"], w=cfg["w"], dt=cfg["dt"],
+                             TransientLength=cfg["TransientLength"], Display=2)
+    ctx = rsvdt.Context(p)
+    ctx.set_operator(A)
+    g = ctx.grid()
+    ctx.set_sketch(synth.complex_normal(A.shape[0], k * g.Nw_eff, 2))
+    capfd.readouterr()
+    ctx.run()
+    out = capfd.readouterr().out
+    assert out.count("Progress percentage: 50%") == 4 and out.count("Progress percentage: 100%") == 4
+    assert out.count("*** Direct action elapsed time = ") == 2
+    assert out.count("*** Adjoint action elapsed time = ") == 2
+    assert f"(k = {k} out of {k})" in out
+    t = ctx.timings()
+    assert t["actions"] == {"direct": 2, "adjoint": 2}
+    assert t["steps"] == 4 * (g.Nt + g.Ns)
+    assert all(v >= 0 for v in t["seconds"].values()) and t["seconds"]["stepping"] > 0
+    ctx.reset_timings()
+    assert ctx.timings()["steps"] == 0
+    ctx.close()
+
+
 def test_diverged_and_state_errors(built_lib):
     import rsvdt
     A, cfg = small_gl()
