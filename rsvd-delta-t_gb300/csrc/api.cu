@@ -960,6 +960,7 @@ rsvdt_status rsvdt_get_block(rsvdt_ctx *ctx, double *Y, int64_t ld, int64_t *row
 rsvdt_status rsvdt_action(rsvdt_ctx *ctx, rsvdt_dir dir) {
   RSVDT_TRY(require_ready(ctx, true));
   const int d = dir == RSVDT_DIRECT ? 1 : 0;
+  NvtxRange range(d ? "rsvdt direct action" : "rsvdt adjoint action");
   const double t0 = now_s();
   ctx->tm.actions[d] += 1;
   rsvdt_status st;
@@ -1085,6 +1086,7 @@ extern "C" {
 rsvdt_status rsvdt_qr_all_freqs(rsvdt_ctx *ctx) {
   RSVDT_TRY(require_ready(ctx, true));
   ++ctx->blk_version;
+  NvtxRange range("rsvdt qr_all_freqs");
   const double t0 = now_s();
   RSVDT_TRY(cholqr2(ctx, ctx->blk, ctx->blk_rows, ctx->Nw_eff, ctx->K, nullptr));
   if (!cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync")) return RSVDT_ERR_CUDA;
@@ -1095,6 +1097,7 @@ rsvdt_status rsvdt_qr_all_freqs(rsvdt_ctx *ctx) {
 static rsvdt_status svd_all_freqs_impl(rsvdt_ctx *ctx, int32_t before_adjoint);
 
 rsvdt_status rsvdt_svd_all_freqs(rsvdt_ctx *ctx, int32_t before_adjoint) {
+  NvtxRange range(before_adjoint ? "rsvdt svd before adjoint" : "rsvdt svd");
   const double t0 = now_s();
   const rsvdt_status st = svd_all_freqs_impl(ctx, before_adjoint);
   if (ctx) ctx->tm.svd += now_s() - t0;

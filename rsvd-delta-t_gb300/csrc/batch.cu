@@ -165,6 +165,7 @@ static rsvdt_status autotune(rsvdt_batch *b, int d) {
 // One action (direct d = 1 or adjoint d = 0) of every problem in `mask`,
 // stages in precision `prec`.
 static rsvdt_status batch_action(rsvdt_batch *b, int d, const std::vector<char> &mask, int prec) {
+  NvtxRange range(d ? "rsvdt batched direct action" : "rsvdt batched adjoint action");
   const size_t np = b->probs.size();
   std::vector<int64_t> rend(np, 0);
   int64_t maxrend = 0;

@@ -9,6 +9,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "rsvdt.h"
 
 namespace rsvdt {
@@ -208,6 +210,16 @@ struct rsvdt_ctx {
 };
 
 namespace rsvdt {
+
+// An NVTX range for the lifetime of the object (one per action, QR, SVD,
+// transient run and batched action), so that profiles group the kernels by
+// phase; costs nothing without a profiler attached.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Stage precision of an action under a params precision: complex128 for the
 // plain form, complex64 for both precision forms.

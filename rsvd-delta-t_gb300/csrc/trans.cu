@@ -372,6 +372,7 @@ rsvdt_status rsvdt_trans_run(rsvdt_ctx *ctx, const rsvdt_trans_params *tp, doubl
   rsvdt_trans_info loc;
   if (!info) info = &loc;
   TR_TRY(trans_grid(ctx, tp, info));
+  NvtxRange range("rsvdt transient run");
   if (!q || !norms) return set_err(ctx, RSVDT_ERR_ARG, "null initial vector or norms");
   const int64_t N = ctx->N, Nw = ctx->Nw;
   const int64_t rend = info->rend, save_mod = tp->save_mod, Ntp = info->Nt_period;

@@ -386,6 +386,67 @@ def test_progress_output_and_phase_timings(built_lib, capfd):
     ctx.close()
 
 
+def test_nan_in_the_operator_is_reported(built_lib):
+    """A NaN injected into A on the host propagates through the stepping and
+    the action returns RSVDT_ERR_DIVERGED with a message (the context stays
+    usable: a clean operator afterwards runs normally)."""
+    import rsvdt
+    A, cfg = small_gl()
+    Abad = A.tolil()
+    Abad[10, 11] = np.nan
+    ctx = make_ctx(Abad.tocsr(), cfg, k=2)
+    F = synth.complex_normal(A.shape[0], 2 * ctx.grid().Nw_eff, 3)
+    ctx.set_sketch(F)
+    with pytest.raises(rsvdt.RsvdtError) as e:
+        ctx.action(1)
+    assert e.value.status == rsvdt.ERR_DIVERGED and "NaN" in str(e.value)
+    ctx.set_operator(A)
+    ctx.set_sketch(F)
+    ctx.action(1)
+    assert np.isfinite(ctx.get_block()).all()
+    ctx.close()
+
+
+def test_3d_gains_match_the_dense_resolvent(built_lib):
+    """The 3D five-field operator (6^3 grid, N = 1080, block-CSR), shifted so
+    that its rightmost eigenvalue (dense eigensolver) sits at -0.05, diagonal
+    W_q = W_f, k = 8, q = 4, transient removal: the leading gain of the whole
+    sequence in the plain and the refinement forms against a dense FP64 SVD
+    of W_q^{1/2} (i w I - A)^{-1} W_f^{-1/2} wherever sigma_1 / sigma_2 > 1.5
+    (the oracle's own run of this case agrees to 1.3e-5 there)."""
+    import rsvdt
+    from rsvdt import workloads
+    br, bc, bl = synth.op3d_blocks(n=6, seed=7, shift=0.0)
+    abscissa = np.linalg.eigvals(synth.bcsr_to_csr(br, bc, bl).toarray()).real.max()
+    br, bc, bl = synth.op3d_blocks(n=6, seed=7, shift=abscissa + 0.05)
+    A = synth.bcsr_to_csr(br, bc, bl)
+    N = A.shape[0]
+    w, Nw, k, q = 0.1, 8, 8, 4
+    dt = 1.0 / workloads.gershgorin_bound_bcsr(br, bc, bl)
+    Wq, Wq_inv = synth.diag_weights(N, seed=11)
+    F = synth.complex_normal(N, k * Nw, 17)
+    res = {}
+    for prec in (rsvdt.PREC_C128, rsvdt.PREC_C64_REFINE):
+        p = rsvdt.default_params(k=k, q=q, Nw=Nw, w=w, dt=dt, TransientLength=2 * 2 * np.pi / w,
+                                 TransientRemoval=1, precision=prec, Display=0)
+        ctx = rsvdt.Context(p)
+        ctx.set_operator_bcsr(br, bc, bl)
+        for which, M in [(rsvdt.W_F_SQRT_INV, Wq_inv), (rsvdt.W_Q_SQRT, Wq), (rsvdt.W_Q_SQRT_INV, Wq_inv)]:
+            ctx.set_weight(which, M)
+        ctx.set_sketch(F)
+        ctx.run()
+        res[prec] = ctx.get_results()[2]
+        ctx.close()
+    om = [oracle.freq_of(i, Nw, w) for i in range(Nw)]
+    Sd, _, _ = oracle.dense_resolvent_svd(A, om, 2, Wq=Wq, Wf_inv=Wq_inv)
+    good = Sd[0] / Sd[1] > 1.5
+    assert good.sum() >= 3
+    for prec, S in res.items():
+        err = (np.abs(S[0, good] - Sd[0, good]) / Sd[0, good]).max()
+        print("3D gains vs dense resolvent, precision form", prec, "max rel err", err)
+        assert err < 1e-4, (prec, err)
+
+
 def test_diverged_and_state_errors(built_lib):
     import rsvdt
     A, cfg = small_gl()
