@@ -558,6 +558,10 @@ def main():
         e.synchronize()
         return s.elapsed_time(e)
 
+    # Everything from here to the end of the complex64 step is inside one NVTX
+    # range, so that a profiler can keep to it (ncu --nvtx --nvtx-include
+    # "rsvdt bench step/").
+    torch.cuda.nvtx.range_push("rsvdt bench step")
     ctx.rk4_reset(rsvdt.DIRECT)
     ctx.rk4_advance(rsvdt.DIRECT, 1, args.warmup)
     ctx.synchronize()
@@ -609,6 +613,7 @@ def main():
     b64 = wl.step_bytes(g.ResRatio, s_c=8)
     st64 = [x / nprof for x in ctx64.rk4_profile(rsvdt.DIRECT, 4 + args.steps, nprof)]
     ctx64.close()
+    torch.cuda.nvtx.range_pop()
 
     ttg = None
     if rank == 0 and not args.no_ttg:

@@ -228,3 +228,63 @@ def dense_resolvent_svd(A, omegas, k: int, Wq=None, Wf_inv=None, B=None, Cm=None
         Us.append(u[:, :k])
         Vs.append(vh.conj().T[:, :k])
     return S, Us, Vs
+
+
+def _sparse_resolvent_one(task):
+    """One frequency of sparse_resolvent_svd (a module-level function so a
+    spawned worker can import it)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+
+    A, om, k, wq, wfi, tol, seed = task
+    N = A.shape[0]
+    lu = spla.splu((1j * om * sp.eye(N, format="csc") - A).tocsc(), permc_spec="MMD_AT_PLUS_A")
+    op = spla.LinearOperator(
+        (N, N), dtype=np.complex128,
+        matvec=lambda x: wq * lu.solve(wfi * x.ravel()),
+        rmatvec=lambda x: np.conj(wfi) * lu.solve(np.conj(wq) * x.ravel(), trans="H"))
+    rng = np.random.default_rng(seed)
+    v0 = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    u, s, vh = spla.svds(op, k=k, tol=tol, v0=v0 / np.linalg.norm(v0))
+    o = np.argsort(-s)
+    return s[o], u[:, o], vh[o].conj().T
+
+
+def sparse_resolvent_svd(A, omegas, k: int, wq=None, wf_inv=None, tol: float = 1e-10, procs: int = 1,
+                         seed: int = 3):
+    """Exact-resolvent oracle for N too large to invert densely: for each w,
+    a sparse LU of (i w I - A) (SuperLU, minimum degree on A^T + A) and
+    Lanczos (ARPACK, scipy svds) on M = diag(wq) (i w I - A)^{-1} diag(wf_inv)
+    for the k leading singular triplets, M and M^H applied through the LU
+    factors. wq, wf_inv: diagonals of W_q^{1/2} and W_f^{-1/2} (None = I).
+    procs > 1 runs the frequencies in a spawned process pool. Returns
+    (S [k, len(omegas)], U list, V list) in the weighted coordinates, like
+    dense_resolvent_svd."""
+    import multiprocessing
+
+    A = A.tocsc()
+    N = A.shape[0]
+    wq = np.ones(N) if wq is None else np.asarray(wq)
+    wf_inv = np.ones(N) if wf_inv is None else np.asarray(wf_inv)
+    tasks = [(A, float(om), k, wq, wf_inv, tol, seed + j) for j, om in enumerate(omegas)]
+    if procs > 1:
+        # Each worker's BLAS (used by SuperLU's supernodes) gets its share of
+        # the cores: oversubscribed spinning BLAS threads are many times slower.
+        procs = min(procs, len(tasks))
+        keys = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
+        saved = {key: os.environ.get(key) for key in keys}
+        for key in keys:
+            os.environ[key] = str(max(1, (os.cpu_count() or 1) // procs))
+        try:
+            with multiprocessing.get_context("spawn").Pool(procs) as pool:
+                res = pool.map(_sparse_resolvent_one, tasks)
+        finally:
+            for key, v in saved.items():
+                if v is None:
+                    os.environ.pop(key, None)
+                else:
+                    os.environ[key] = v
+    else:
+        res = [_sparse_resolvent_one(t) for t in tasks]
+    S = np.stack([r[0] for r in res], axis=1)
+    return S, [r[1] for r in res], [r[2] for r in res]

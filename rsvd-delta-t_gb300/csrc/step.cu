@@ -62,6 +62,32 @@ struct StepArgs {
   int64_t rend;  // last step of this problem's action (batched stepping)
 };
 
+// Programmatic dependent launch: a stage kernel is launched while the one
+// before it is still running (its launch latency overlaps that kernel's
+// work), and waits here until that kernel has completed and its writes are
+// visible, before it touches any state. Without a programmatic dependency
+// (an ordinary launch) the wait returns at once.
+__device__ __forceinline__ void pdl_wait_and_release() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launches kernel k with the programmatic-serialization attribute on st.
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*k)(KArgs...), int grid, int threads, size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // Half-step forcing indices of step i (SourceCode/TSRK4.c:21-26). For the
 // adjoint, fmod(1e6*Ns - 1 - m, 2Ns) equals (-1 - m) mod 2Ns because 1e6*Ns
 // is a multiple of 2Ns.
@@ -204,6 +230,7 @@ __device__ __forceinline__ void row_product(const StepArgs<Z> &P, int64_t n, int
 
 template <class Z, int S>
 __global__ void __launch_bounds__(256) k_stage(const StepArgs<Z> P) {
+  pdl_wait_and_release();
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t NK = P.N * P.K;
   int64_t i = (S == 1) ? P.step[0] : P.step[1];
@@ -302,6 +329,7 @@ static const int kRowThreads = 128;
 // registers for the forcing synthesis.
 template <class Z, int K, int KP, int S>
 __global__ void __launch_bounds__(kRowThreads, S == 1 ? 1 : 8) k_bstage(const StepArgs<Z> P) {
+  pdl_wait_and_release();
   constexpr int L = K / KP;
   constexpr int BPW = 32 / L;
   extern __shared__ unsigned char smem_raw[];
@@ -591,6 +619,7 @@ __device__ __forceinline__ void forcing_row(const StepArgs<Z> &P, int64_t n, con
 // lane-group kernel above leaves lanes idle for complex128 row groups.
 template <class Z, int K, int S>
 __global__ void __launch_bounds__(kRowThreads) k_rstage(const StepArgs<Z> P) {
+  pdl_wait_and_release();
   extern __shared__ unsigned char smem_raw[];
   Z *e2 = reinterpret_cast<Z *>(smem_raw);  // phasor rows of this step (stage 1)
   Z *e3 = e2 + P.Nw;
@@ -788,18 +817,18 @@ static void launch_bstage(int stage, const StepArgs<Z> &P, cudaStream_t st) {
   if constexpr (sizeof(Z) == 16) {
     const int gr = grid_for(P.N, kRowThreads);
     switch (stage) {
-      case 1: k_rstage<Z, K, 1><<<gr, kRowThreads, sm, st>>>(P); break;
-      case 2: k_rstage<Z, K, 2><<<gr, kRowThreads, 0, st>>>(P); break;
-      case 3: k_rstage<Z, K, 3><<<gr, kRowThreads, 0, st>>>(P); break;
-      default: k_rstage<Z, K, 4><<<gr, kRowThreads, 0, st>>>(P); break;
+      case 1: launch_pdl(k_rstage<Z, K, 1>, gr, kRowThreads, sm, st, P); break;
+      case 2: launch_pdl(k_rstage<Z, K, 2>, gr, kRowThreads, 0, st, P); break;
+      case 3: launch_pdl(k_rstage<Z, K, 3>, gr, kRowThreads, 0, st, P); break;
+      default: launch_pdl(k_rstage<Z, K, 4>, gr, kRowThreads, 0, st, P); break;
     }
     return;
   }
   switch (stage) {
-    case 1: k_bstage<Z, K, KP, 1><<<g, kRowThreads, sm, st>>>(P); break;
-    case 2: k_bstage<Z, K, KP, 2><<<g, kRowThreads, 0, st>>>(P); break;
-    case 3: k_bstage<Z, K, KP, 3><<<g, kRowThreads, 0, st>>>(P); break;
-    default: k_bstage<Z, K, KP, 4><<<g, kRowThreads, 0, st>>>(P); break;
+    case 1: launch_pdl(k_bstage<Z, K, KP, 1>, g, kRowThreads, sm, st, P); break;
+    case 2: launch_pdl(k_bstage<Z, K, KP, 2>, g, kRowThreads, 0, st, P); break;
+    case 3: launch_pdl(k_bstage<Z, K, KP, 3>, g, kRowThreads, 0, st, P); break;
+    default: launch_pdl(k_bstage<Z, K, KP, 4>, g, kRowThreads, 0, st, P); break;
   }
 }
 
@@ -823,10 +852,10 @@ static void launch_stage(int stage, const StepArgs<Z> &P, cudaStream_t st) {
   const int th = 256;
   const int g = grid_for(P.N * P.K, th);
   switch (stage) {
-    case 1: k_stage<Z, 1><<<g, th, 0, st>>>(P); break;
-    case 2: k_stage<Z, 2><<<g, th, 0, st>>>(P); break;
-    case 3: k_stage<Z, 3><<<g, th, 0, st>>>(P); break;
-    default: k_stage<Z, 4><<<g, th, 0, st>>>(P); break;
+    case 1: launch_pdl(k_stage<Z, 1>, g, th, 0, st, P); break;
+    case 2: launch_pdl(k_stage<Z, 2>, g, th, 0, st, P); break;
+    case 3: launch_pdl(k_stage<Z, 3>, g, th, 0, st, P); break;
+    default: launch_pdl(k_stage<Z, 4>, g, th, 0, st, P); break;
   }
 }
 
@@ -910,10 +939,10 @@ static rsvdt_status run_steps_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t nst
 // thread's forcing synthesis, which the split shortens FS times.
 int step_lanes(const rsvdt_ctx *ctx) {
   if (ctx->lanes_override > 0) return ctx->lanes_override;
-  // Measured on GB300: 8 lanes take the 500-node Ginzburg-Landau step (5000
-  // rows x test vectors) from 32 to 27 us; problems a few times larger are
-  // faster with one lane per row.
-  return ctx->N * ctx->Ks <= 8192 ? 8 : 1;
+  // Measured on GB300, the 500-node Ginzburg-Landau step (5000 rows x test
+  // vectors): 32 us with one lane, 25.7 with 8, 24.0 with 4; problems a few
+  // times larger are faster with one lane per row.
+  return ctx->N * ctx->Ks <= 8192 ? 4 : 1;
 }
 
 static const int kSmallThreads = 128;
@@ -1201,6 +1230,7 @@ __device__ __forceinline__ void group_sum(Z &v) {
 template <class Z, int S, int FS>
 __global__ void __launch_bounds__(256) k_stage_batched(const StepArgs<Z> *__restrict__ probs,
                                                        const int2 *__restrict__ work, int64_t *step) {
+  pdl_wait_and_release();
   const int2 wk = work[blockIdx.x];
   const StepArgs<Z> &P = probs[wk.x];
   const int64_t i = (S == 1) ? step[0] : step[1];
@@ -1280,10 +1310,10 @@ template <class Z, int FS>
 static void launch_batched_fs(cudaStream_t st, const void *args, const int2 *work, int nwork, int threads,
                               int64_t *step) {
   const StepArgs<Z> *P = (const StepArgs<Z> *)args;
-  k_stage_batched<Z, 1, FS><<<nwork, threads, 0, st>>>(P, work, step);
-  k_stage_batched<Z, 2, FS><<<nwork, threads, 0, st>>>(P, work, step);
-  k_stage_batched<Z, 3, FS><<<nwork, threads, 0, st>>>(P, work, step);
-  k_stage_batched<Z, 4, FS><<<nwork, threads, 0, st>>>(P, work, step);
+  launch_pdl(k_stage_batched<Z, 1, FS>, nwork, threads, 0, st, P, work, step);
+  launch_pdl(k_stage_batched<Z, 2, FS>, nwork, threads, 0, st, P, work, step);
+  launch_pdl(k_stage_batched<Z, 3, FS>, nwork, threads, 0, st, P, work, step);
+  launch_pdl(k_stage_batched<Z, 4, FS>, nwork, threads, 0, st, P, work, step);
 }
 
 template <class Z>

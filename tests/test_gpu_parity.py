@@ -293,7 +293,7 @@ def test_bcsr_matches_csr_and_oracle(built_lib, lanes):
     ctx_c = make_ctx(Acsr, cfg, k=k)
     ctx_b.set_lanes_per_row(lanes)
     ctx_c.set_lanes_per_row(lanes)
-    assert ctx_b.lanes_per_row() == (1 if lanes == 1 else 8)
+    assert ctx_b.lanes_per_row() == (1 if lanes == 1 else 4)
     g = ctx_b.grid()
     F = synth.complex_normal(Acsr.shape[0], k * g.Nw_eff, 9)
     for d in (1, 0):
