@@ -165,6 +165,19 @@ rsvdt_status rsvdt_svd_all_freqs(rsvdt_ctx *ctx, int32_t before_adjoint);
 /* Power iteration loop (SourceCode/PowerIterationRK4.c:8-36). */
 rsvdt_status rsvdt_power_iteration(rsvdt_ctx *ctx);
 
+/* Checkpoint hook of the power iteration. The reference's only resume path
+ * is to feed a forcing matrix back through InputForcingDir
+ * (SourceCode/CreateRandomMat.c:10-11,23-31); this hook produces such a
+ * matrix. fn(user, sweep, ctx) is called after the second QR of every sweep
+ * (sweep = 1..q), when the working block holds the forcing of that sweep's
+ * direct action; fn may read it with rsvdt_get_block. Setting that block as
+ * the sketch (rsvdt_set_sketch, or InputForcingDir in the driver) and
+ * running with q - sweep power iterations continues the sequence exactly
+ * (identical results). A non-zero return stops rsvdt_power_iteration and
+ * rsvdt_run with RSVDT_ERR_STATE. fn = NULL removes the hook. */
+typedef int (*rsvdt_checkpoint_fn)(void *user, int32_t sweep, rsvdt_ctx *ctx);
+rsvdt_status rsvdt_set_checkpoint(rsvdt_ctx *ctx, rsvdt_checkpoint_fn fn, void *user);
+
 /* The whole RSVD-Delta-t sequence of SourceCode/main.c:134-144 on the
  * current sketch. */
 rsvdt_status rsvdt_run(rsvdt_ctx *ctx);
@@ -230,6 +243,11 @@ int32_t rsvdt_get_lanes_per_row(const rsvdt_ctx *ctx);
  * with Display >= 1 the library prints them too. */
 rsvdt_status rsvdt_get_timings(const rsvdt_ctx *ctx, char *json, int64_t len);
 rsvdt_status rsvdt_reset_timings(rsvdt_ctx *ctx);
+
+/* 1 for the bounds-checked debug build (compiled with RSVDT_DEBUG: the
+ * stage kernels check every gathered column and ring slot, skip an access
+ * that fails and make the action return RSVDT_ERR_ARG), 0 otherwise. */
+int32_t rsvdt_debug_build(void);
 
 /* Free and total memory of the current CUDA device, in bytes (for callers
  * deciding on the capacity mode before they create the buffers). */

@@ -1025,6 +1025,7 @@ static rsvdt_status weights_after(rsvdt_ctx *ctx, int d) {
     RSVDT_TRY(weight_step(ctx, ctx->WH[RSVDT_B], ctx->blk_rows));
     RSVDT_TRY(weight_step(ctx, ctx->WH[RSVDT_W_F_SQRT_INV], ctx->blk_rows));
   }
+  RSVDT_TRY(debug_index_status(ctx));
   bool ok = true;
   RSVDT_TRY(check_finite(ctx, ctx->blk, ctx->blk_rows * ctx->Nw_eff * ctx->K, &ok));
   if (!ok) return set_err(ctx, RSVDT_ERR_DIVERGED, "NaN or Inf in the %s action's response", d ? "direct" : "adjoint");
@@ -1152,8 +1153,17 @@ rsvdt_status rsvdt_power_iteration(rsvdt_ctx *ctx) {
     RSVDT_TRY(rsvdt_qr_all_freqs(ctx));
     RSVDT_TRY(rsvdt_action(ctx, RSVDT_ADJOINT));
     RSVDT_TRY(rsvdt_qr_all_freqs(ctx));
+    if (ctx->ckpt_fn && ctx->ckpt_fn(ctx->ckpt_user, (int32_t)(iq + 1), ctx) != 0)
+      return set_err(ctx, RSVDT_ERR_STATE, "stopped by the checkpoint callback after power sweep %d", (int)iq + 1);
     RSVDT_TRY(rsvdt_action(ctx, RSVDT_DIRECT));
   }
+  return RSVDT_OK;
+}
+
+rsvdt_status rsvdt_set_checkpoint(rsvdt_ctx *ctx, rsvdt_checkpoint_fn fn, void *user) {
+  if (!ctx) return RSVDT_ERR_ARG;
+  ctx->ckpt_fn = fn;
+  ctx->ckpt_user = fn ? user : nullptr;
   return RSVDT_OK;
 }
 
@@ -1265,7 +1275,16 @@ rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t 
 
 rsvdt_status rsvdt_synchronize(rsvdt_ctx *ctx) {
   if (!ctx) return RSVDT_ERR_ARG;
-  return cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
+  if (!cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync")) return RSVDT_ERR_CUDA;
+  return debug_index_status(ctx);
+}
+
+int32_t rsvdt_debug_build(void) {
+#ifdef RSVDT_DEBUG
+  return 1;
+#else
+  return 0;
+#endif
 }
 
 void *rsvdt_stream(rsvdt_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }

@@ -199,6 +199,9 @@ struct rsvdt_ctx {
   // step_lanes): lanes per row (0 = chosen from the size), the argument
   // blocks of both directions, the work list and the cached graphs.
   int lanes_override = 0;
+  // rsvdt_set_checkpoint: called after the second QR of every power sweep.
+  rsvdt_checkpoint_fn ckpt_fn = nullptr;
+  void *ckpt_user = nullptr;
   void *small_args = nullptr;
   int2 *small_work = nullptr;
   int small_nwork = 0;
@@ -261,6 +264,7 @@ void launch_set_step(cudaStream_t st, int64_t *step, int64_t i);
 rsvdt_status launch_unforced_steps(rsvdt_ctx *ctx, int dir, z128 *cols, int64_t ncols,
                                    int64_t nsteps);
 int step_lanes(const rsvdt_ctx *ctx);
+rsvdt_status debug_index_status(rsvdt_ctx *ctx);
 rsvdt_status launch_trans_steps(rsvdt_ctx *ctx, double dt, z128 *y, z128 *work, int64_t nsteps,
                                 cudaGraphExec_t *graph);
 // dense.cu

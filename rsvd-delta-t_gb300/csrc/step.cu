@@ -88,6 +88,18 @@ static void launch_pdl(void (*k)(KArgs...), int grid, int threads, size_t smem, 
   cudaLaunchKernelEx(&cfg, k, args...);
 }
 
+// Index checks of the debug build (RSVDT_DEBUG): a failed check sets its
+// site's bit in g_index_faults and skips the access; the host reads and
+// clears the word after every action (debug_index_status). Sites: 0 = CSR
+// column, 1 = block column, 2 = ring slot. In the release build the checks
+// compile to nothing.
+#ifdef RSVDT_DEBUG
+__device__ unsigned int g_index_faults;
+#define RSVDT_CHECK_INDEX(cond, site) ((cond) || (atomicOr(&g_index_faults, 1u << (site)), false))
+#else
+#define RSVDT_CHECK_INDEX(cond, site) true
+#endif
+
 // Half-step forcing indices of step i (SourceCode/TSRK4.c:21-26). For the
 // adjoint, fmod(1e6*Ns - 1 - m, 2Ns) equals (-1 - m) mod 2Ns because 1e6*Ns
 // is a multiple of 2Ns.
@@ -205,8 +217,10 @@ __device__ __forceinline__ void row_product(const StepArgs<Z> &P, int64_t n, int
   if (P.bs == 0) {
     int32_t b = __ldg(P.rowptr + n), e = __ldg(P.rowptr + n + 1);
     for (int32_t j = b; j < e; ++j) {
+      const int32_t cj = __ldg(P.col + j);
+      if (!RSVDT_CHECK_INDEX(cj >= 0 && cj < P.N, 0)) continue;
       const Z a = P.val[j];
-      const Z v = x[(int64_t)__ldg(P.col + j) * K + kc];
+      const Z v = x[(int64_t)cj * K + kc];
       zmac(acc, a, v);
     }
   } else {
@@ -215,7 +229,9 @@ __device__ __forceinline__ void row_product(const StepArgs<Z> &P, int64_t n, int
     const int r = (int)(n - br * bs);
     int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
     for (int32_t j = b; j < e; ++j) {
-      const int64_t c0 = (int64_t)__ldg(P.col + j) * bs;
+      const int32_t cb = __ldg(P.col + j);
+      if (!RSVDT_CHECK_INDEX(cb >= 0 && cb < P.N / bs, 1)) continue;
+      const int64_t c0 = (int64_t)cb * bs;
       const Z *blkrow = P.val + (int64_t)j * P.bstride + r * bs;
       for (int c = 0; c < bs; ++c) {
         const Z a = blkrow[c];
@@ -266,7 +282,7 @@ __global__ void __launch_bounds__(256) k_stage(const StepArgs<Z> P) {
     const Z ynew = zaxpy(P.dt_6, k, P.acc[t]);
     P.y[t] = ynew;
     const int64_t p = P.ring ? ring_slot(P.dir, i, P.Nt, P.R, P.Nstore) : -1;
-    if (p >= 0) P.ring[p * NK + t] = ynew;
+    if (p >= 0 && RSVDT_CHECK_INDEX(p < P.Nstore, 2)) P.ring[p * NK + t] = ynew;
     if (t == 0) P.step[0] = i + 1;
   }
 }
@@ -367,7 +383,9 @@ __global__ void __launch_bounds__(kRowThreads, S == 1 ? 1 : 8) k_bstage(const St
   {
     const int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
     for (int32_t j = b; j < e; ++j) {
-      const int64_t c0 = (int64_t)__ldg(P.col + j) * 5;
+      const int32_t cb = __ldg(P.col + j);
+      if (!RSVDT_CHECK_INDEX(cb >= 0 && cb < P.N / 5, 1)) continue;
+      const int64_t c0 = (int64_t)cb * 5;
       const Z *blk = P.val + (int64_t)j * P.bstride;
       if constexpr (S == 4 && sizeof(Z) == 8) {
         // The padded 26-value block as 13 aligned 16-byte loads.
@@ -505,7 +523,7 @@ __global__ void __launch_bounds__(kRowThreads, S == 1 ? 1 : 8) k_bstage(const St
 #pragma unroll
       for (int p = 0; p < KP; ++p) av[p] = zaxpy(P.dt_6, k[r][p], av[p]);
       st_chunk<Z, KP>(P.y + base + r * K, av);
-      if (ps >= 0) st_chunk<Z, KP>(P.ring + ps * P.N * K + base + r * K, av);
+      if (ps >= 0 && RSVDT_CHECK_INDEX(ps < P.Nstore, 2)) st_chunk<Z, KP>(P.ring + ps * P.N * K + base + r * K, av);
     }
     if (br == 0 && q == 0) P.step[0] = i + 1;
   }
@@ -651,7 +669,9 @@ __global__ void __launch_bounds__(kRowThreads) k_rstage(const StepArgs<Z> P) {
     const int r = (int)(n - br * 5);
     const int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
     for (int32_t j = b; j < e; ++j) {
-      const int64_t c0 = (int64_t)__ldg(P.col + j) * 5;
+      const int32_t cb = __ldg(P.col + j);
+      if (!RSVDT_CHECK_INDEX(cb >= 0 && cb < P.N / 5, 1)) continue;
+      const int64_t c0 = (int64_t)cb * 5;
       const Z *arow = P.val + (int64_t)j * P.bstride + r * 5;
       Z a[5];
 #pragma unroll
@@ -700,7 +720,7 @@ __global__ void __launch_bounds__(kRowThreads) k_rstage(const StepArgs<Z> P) {
     for (int q = 0; q < K; ++q) av[q] = zaxpy(P.dt_6, k[q], av[q]);
     st_row<Z, K>(P.y + n * K, av);
     const int64_t p = P.ring ? ring_slot(P.dir, i, P.Nt, P.R, P.Nstore) : -1;
-    if (p >= 0) st_row<Z, K>(P.ring + (p * P.N + n) * K, av);
+    if (p >= 0 && RSVDT_CHECK_INDEX(p < P.Nstore, 2)) st_row<Z, K>(P.ring + (p * P.N + n) * K, av);
     if (n == 0) P.step[0] = i + 1;
   }
 }
@@ -1183,6 +1203,26 @@ rsvdt_status launch_trans_steps(rsvdt_ctx *ctx, double dt, z128 *y, z128 *work, 
   return RSVDT_OK;
 }
 
+// Reads and clears the debug build's index-check word (release build: OK).
+rsvdt_status debug_index_status(rsvdt_ctx *ctx) {
+#ifdef RSVDT_DEBUG
+  unsigned int f = 0;
+  if (!cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ||
+      !cuda_ok(ctx, cudaMemcpyFromSymbol(&f, g_index_faults, sizeof f), "index check word"))
+    return RSVDT_ERR_CUDA;
+  if (f) {
+    const unsigned int zero = 0;
+    if (!cuda_ok(ctx, cudaMemcpyToSymbol(g_index_faults, &zero, sizeof zero), "index check word"))
+      return RSVDT_ERR_CUDA;
+    return set_err(ctx, RSVDT_ERR_ARG, "debug build: an index check failed in a stage kernel (sites 0x%x: "
+                   "1 = CSR column, 2 = block column, 4 = ring slot)", f);
+  }
+#else
+  (void)ctx;
+#endif
+  return RSVDT_OK;
+}
+
 }  // namespace rsvdt
 
 // ------------------------------------------------------ batched stepping
@@ -1204,14 +1244,20 @@ __device__ __forceinline__ void row_product_split(const StepArgs<Z> &P, int64_t 
   const int K = P.K;
   if (P.bs == 0) {
     const int32_t b = __ldg(P.rowptr + n), e = __ldg(P.rowptr + n + 1);
-    for (int32_t j = b + fsub; j < e; j += FS) zmac(acc, P.val[j], x[(int64_t)__ldg(P.col + j) * K + kc]);
+    for (int32_t j = b + fsub; j < e; j += FS) {
+      const int32_t cj = __ldg(P.col + j);
+      if (!RSVDT_CHECK_INDEX(cj >= 0 && cj < P.N, 0)) continue;
+      zmac(acc, P.val[j], x[(int64_t)cj * K + kc]);
+    }
   } else {
     const int bs = P.bs;
     const int64_t br = n / bs;
     const int r = (int)(n - br * bs);
     const int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
     for (int32_t j = b + fsub; j < e; j += FS) {
-      const int64_t c0 = (int64_t)__ldg(P.col + j) * bs;
+      const int32_t cb = __ldg(P.col + j);
+      if (!RSVDT_CHECK_INDEX(cb >= 0 && cb < P.N / bs, 1)) continue;
+      const int64_t c0 = (int64_t)cb * bs;
       const Z *blkrow = P.val + (int64_t)j * P.bstride + r * bs;
       for (int c = 0; c < bs; ++c) zmac(acc, blkrow[c], x[(c0 + c) * K + kc]);
     }
@@ -1284,7 +1330,7 @@ __global__ void __launch_bounds__(256) k_stage_batched(const StepArgs<Z> *__rest
     const Z ynew = zaxpy(P.dt_6, k, P.acc[t]);
     P.y[t] = ynew;
     const int64_t p = P.ring ? ring_slot(P.dir, i, P.Nt, P.R, P.Nstore) : -1;
-    if (p >= 0) P.ring[p * NK + t] = ynew;
+    if (p >= 0 && RSVDT_CHECK_INDEX(p < P.Nstore, 2)) P.ring[p * NK + t] = ynew;
   }
 }
 

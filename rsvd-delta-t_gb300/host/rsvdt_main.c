@@ -163,6 +163,9 @@ typedef struct {
   char folder[PATHLEN];
   int wflag[5];
   int input_forcing, trans_run, save_opt;
+  /* SaveResumeQ (no counterpart in the reference): write the forcing of
+   * every power sweep's direct action as a resume point. */
+  int save_resume;
   int64_t rand_seed;
   /* Transient simulation (SourceCode/Variables.h TransRun_vars). */
   int trans_ic_flg;
@@ -210,6 +213,7 @@ static void read_user_input(rsvdt_params *p, drv_t *d) {
     d->trans_run = 0;
     warn_default_i("TransRun", 0);
   }
+  if (!get_bool("SaveResumeQ", &d->save_resume)) d->save_resume = 0;
   if (!get_bool("TransientRemoval", &b)) {
     b = 0;
     warn_default_i("TransientRemoval", 0);
@@ -290,6 +294,35 @@ static void read_user_input(rsvdt_params *p, drv_t *d) {
     warn_default_i("TransPeriods", 1);
   }
   printf("\n");
+}
+
+/* Resume point of power sweep j: the block that the sweep's direct action
+ * takes as its forcing, written as Q_resume_sweep<j> in the results folder
+ * (dense, MatView layout), readable through InputForcingDir; a run from it
+ * with q - j power iterations continues this run exactly. */
+typedef struct {
+  const drv_t *d;
+  int64_t rows, cols, q;
+} resume_t;
+
+static int write_resume_point(void *user, int32_t sweep, rsvdt_ctx *ctx) {
+  const resume_t *rs = (const resume_t *)user;
+  double *Q = (double *)malloc(sizeof(double) * 2 * (size_t)rs->rows * (size_t)rs->cols);
+  if (!Q) {
+    fprintf(stderr, "out of memory for the resume point\n");
+    return 1;
+  }
+  char path[PATHLEN], name[64], err[512];
+  int rc = rsvdt_get_block(ctx, Q, rs->rows, NULL) != RSVDT_OK;
+  snprintf(name, sizeof name, "Q_resume_sweep%d", (int)sweep);
+  join(path, rs->d->folder, name);
+  if (!rc && pb_write_dense(path, Q, rs->rows, rs->cols, rs->rows, err, sizeof err)) {
+    fprintf(stderr, "%s\n", err);
+    rc = 1;
+  }
+  free(Q);
+  if (!rc) printf("Resume point (InputForcingDir with q = %d): %s\n", (int)(rs->q - sweep), path);
+  return rc;
 }
 
 /* SourceCode/CreateResultsDir.c:20-30. */
@@ -527,6 +560,8 @@ int main(int argc, char **argv) {
     check(ctx, rsvdt_random_sketch(ctx, (uint64_t)d.rand_seed), "random sketch");
   }
   create_results_dir(&d, "ResolventModes_");
+  resume_t rs = {&d, g.Nb, k * g.Nw_eff, p.q};
+  if (d.save_resume) check(ctx, rsvdt_set_checkpoint(ctx, write_resume_point, &rs), "checkpoint");
 
   printf("\n********************************************\n*************** RSVD-\\Delta t **************\n"
          "********************************************\n");

@@ -35,7 +35,8 @@ EXPORTED = [
     "rsvdt_default_params", "rsvdt_create", "rsvdt_destroy", "rsvdt_last_error",
     "rsvdt_set_operator", "rsvdt_set_operator_bcsr", "rsvdt_set_weight", "rsvdt_get_grid",
     "rsvdt_set_sketch", "rsvdt_random_sketch", "rsvdt_get_block", "rsvdt_action",
-    "rsvdt_qr_all_freqs", "rsvdt_svd_all_freqs", "rsvdt_power_iteration", "rsvdt_run",
+    "rsvdt_qr_all_freqs", "rsvdt_svd_all_freqs", "rsvdt_power_iteration", "rsvdt_set_checkpoint", "rsvdt_run",
+    "rsvdt_debug_build",
     "rsvdt_get_results", "rsvdt_rk4_steps", "rsvdt_rk4_reset", "rsvdt_rk4_advance",
     "rsvdt_rk4_profile", "rsvdt_synchronize", "rsvdt_stream", "rsvdt_launch_count",
     "rsvdt_qr_all_freqs_noalloc", "rsvdt_trans_grid", "rsvdt_trans_run",
@@ -98,6 +99,7 @@ TRANS_DONE, TRANS_NAN, TRANS_DIVERGED, TRANS_CONVERGED = range(4)
 TRANS_SNAPSHOT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.c_int64)
 TRANS_ESTIMATE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                 C.c_int64)
+CHECKPOINT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32, C.c_void_p)
 
 
 class RsvdtError(RuntimeError):
@@ -110,11 +112,13 @@ _lib = None
 
 
 def load_library(path: str | None = None) -> C.CDLL:
-    """Loads lib/librsvdt.so; raises if it has not been built."""
+    """Loads lib/librsvdt.so (or the file named by the RSVDT_LIBRARY
+    environment variable, e.g. the debug build); raises if it has not been
+    built."""
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    path = path or os.environ.get("RSVDT_LIBRARY") or LIB_PATH
     if not os.path.exists(path):
         raise RuntimeError(f"CUDA library {path} is missing: run build.build_library() first")
     lib = C.CDLL(path)
@@ -138,6 +142,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "rsvdt_qr_all_freqs": (C.c_int, [vp]),
         "rsvdt_svd_all_freqs": (C.c_int, [vp, C.c_int32]),
         "rsvdt_power_iteration": (C.c_int, [vp]),
+        "rsvdt_set_checkpoint": (C.c_int, [vp, C.c_void_p, C.c_void_p]),
+        "rsvdt_debug_build": (C.c_int32, []),
         "rsvdt_run": (C.c_int, [vp]),
         "rsvdt_get_results": (C.c_int, [vp, d, i64, d, i64, d]),
         "rsvdt_rk4_steps": (C.c_int, [vp, C.c_int, i64, i64, d, d]),
@@ -307,6 +313,25 @@ class Context:
 
     def power_iteration(self) -> None:
         self._check(self._lib.rsvdt_power_iteration(self._h))
+
+    def set_checkpoint(self, fn) -> None:
+        """fn(sweep) is called after the second QR of every power sweep
+        (rsvdt_set_checkpoint); it may read the block with get_block(). A
+        true return value stops the run (RsvdtError, ERR_STATE). None
+        removes the hook."""
+        if fn is None:
+            self._ckpt = None
+            self._check(self._lib.rsvdt_set_checkpoint(self._h, None, None))
+            return
+
+        def tramp(user, sweep, ctx):
+            try:
+                return 1 if fn(int(sweep)) else 0
+            except Exception:
+                return 1
+
+        self._ckpt = CHECKPOINT_FN(tramp)
+        self._check(self._lib.rsvdt_set_checkpoint(self._h, C.cast(self._ckpt, C.c_void_p), None))
 
     def run(self) -> None:
         self._check(self._lib.rsvdt_run(self._h))

@@ -20,6 +20,8 @@ INCLUDE = os.path.join(REPO_ROOT, "include")
 LIB_DIR = os.path.join(PKG_ROOT, "lib")
 BIN_DIR = os.path.join(PKG_ROOT, "bin")
 LIB_PATH = os.path.join(LIB_DIR, "librsvdt.so")
+# The bounds-checked debug build (RSVDT_DEBUG), used by the tests only.
+DEBUG_LIB_PATH = os.path.join(LIB_DIR, "librsvdt_debug.so")
 MAIN_PATH = os.path.join(BIN_DIR, "rsvdt_main")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -47,11 +49,15 @@ def _stale(target: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build_library(force: bool = False, verbose: bool = False) -> str:
-    """Compiles csrc/*.cu into lib/librsvdt.so (static CUDA runtime)."""
+def build_library(force: bool = False, verbose: bool = False, debug: bool = False) -> str:
+    """Compiles csrc/*.cu into lib/librsvdt.so (static CUDA runtime); with
+    debug=True, into lib/librsvdt_debug.so with the stage kernels' index
+    checks (-DRSVDT_DEBUG)."""
     os.makedirs(LIB_DIR, exist_ok=True)
-    obj_dir = os.path.join(LIB_DIR, "obj")
+    obj_dir = os.path.join(LIB_DIR, "obj_debug" if debug else "obj")
     os.makedirs(obj_dir, exist_ok=True)
+    out_path = DEBUG_LIB_PATH if debug else LIB_PATH
+    flags = NVCC_FLAGS + (["-DRSVDT_DEBUG"] if debug else [])
     nvcc = _nvcc()
     headers = [os.path.join(CSRC, "common.cuh"), os.path.join(INCLUDE, "rsvdt.h")]
     jobs = []
@@ -61,15 +67,15 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
         o = os.path.join(obj_dir, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, "-c", s, "-o", o])
+            jobs.append([nvcc, *ARCH, *flags, "-c", s, "-o", o])
     if jobs:
         with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
             list(ex.map(_run, jobs))
-    if force or jobs or _stale(LIB_PATH, objs):
-        _run([nvcc, *ARCH, "-shared", "-o", LIB_PATH, *objs, "-cudart", "static"])
+    if force or jobs or _stale(out_path, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", out_path, *objs, "-cudart", "static"])
     if verbose:
-        print("built", LIB_PATH)
-    return LIB_PATH
+        print("built", out_path)
+    return out_path
 
 
 def build_host(force: bool = False) -> str | None:

@@ -447,6 +447,41 @@ def test_3d_gains_match_the_dense_resolvent(built_lib):
         assert err < 1e-4, (prec, err)
 
 
+def test_checkpoint_resumes_exactly(built_lib):
+    """rsvdt_set_checkpoint: the block read at power sweep j, set as the
+    sketch of a run with q - j sweeps, reproduces the uninterrupted run's
+    gains and modes bit for bit; a callback returning true stops the run."""
+    import rsvdt
+    A, cfg = small_gl()
+    k, q = 3, 2
+    ctx = make_ctx(A, cfg, k=k, q=q, tr=True)
+    F = synth.complex_normal(A.shape[0], k * ctx.grid().Nw_eff, 23)
+    saved = {}
+
+    def keep(sweep):
+        saved[sweep] = ctx.get_block()
+        return False
+
+    ctx.set_checkpoint(keep)
+    ctx.set_sketch(F)
+    ctx.run()
+    U, V, S = ctx.get_results()
+    assert sorted(saved) == [1, 2]
+    ctx.set_checkpoint(lambda sweep: sweep == 1)
+    ctx.set_sketch(F)
+    with pytest.raises(rsvdt.RsvdtError) as e:
+        ctx.run()
+    assert e.value.status == rsvdt.ERR_STATE and "checkpoint" in str(e.value)
+    ctx.close()
+    for sweep, Q in saved.items():
+        c2 = make_ctx(A, cfg, k=k, q=q - sweep, tr=True)
+        c2.set_sketch(Q)
+        c2.run()
+        U2, V2, S2 = c2.get_results()
+        c2.close()
+        assert np.array_equal(S2, S) and np.array_equal(U2, U) and np.array_equal(V2, V), sweep
+
+
 def test_diverged_and_state_errors(built_lib):
     import rsvdt
     A, cfg = small_gl()

@@ -163,3 +163,28 @@ def test_transient_run_writes_the_reference_files(driver, tmp_path):
         assert np.abs(gu - upd).max() < 1e-12
     assert (folder / "variables.yaml").exists()
     assert "Transient run" in r.stdout and "Total snapshots to be saved" in r.stdout
+
+
+@pytest.mark.gpu
+def test_resume_point_continues_the_run(driver, tmp_path):
+    """SaveResumeQ writes the forcing of every power sweep's direct action;
+    fed back through InputForcingDir with q reduced by the sweep, it gives
+    the same gains as the uninterrupted run."""
+    A = synth.gl_operator(64, mu0=0.2)
+    petsc_io.write_mat(str(tmp_path / "A"), A)
+    F = synth.complex_normal(64, 2 * 8, 19)
+    petsc_io.write_mat(str(tmp_path / "F"), F)
+    r = run(driver, tmp_path, InputForcingFlg="true", InputForcingDir="F", q=2, SaveResumeQ="true",
+            TransientRemoval="true")
+    assert r.returncode == 0, r.stderr + r.stdout
+    first = tmp_path / "ResolventModes_0"
+    assert "Resume point (InputForcingDir with q = 1)" in r.stdout
+    S_full = petsc_io.read_mat(str(first / "S_hat")).toarray()
+    for sweep in (1, 2):
+        Q = petsc_io.read_mat(str(first / f"Q_resume_sweep{sweep}"))
+        assert Q.shape == (64, 16)
+        r = run(driver, tmp_path, InputForcingFlg="true", InputForcingDir=f"ResolventModes_0/Q_resume_sweep{sweep}",
+                q=2 - sweep, TransientRemoval="true")
+        assert r.returncode == 0, r.stderr + r.stdout
+        S = petsc_io.read_mat(str(tmp_path / f"ResolventModes_{sweep}" / "S_hat")).toarray()
+        assert np.array_equal(S, S_full), sweep
