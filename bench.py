@@ -171,6 +171,7 @@ def time_to_gains(n: int, seed: int = 4321):
             ctx.rk4_advance(d, 1, 32)
         ctx.random_sketch(seed)
         ctx.synchronize()
+        ctx.reset_timings()
         t0 = time.perf_counter()
         ctx.run()
         S = ctx.get_results(U=False, V=False)[2]
@@ -178,6 +179,7 @@ def time_to_gains(n: int, seed: int = 4321):
         U = ctx.get_result_cols([iw * wl.k for iw in range(wl.Nw)], U=True, V=False)[0]
         res[name] = (U, None, S)
         out[name + "_s"] = round(t, 4)
+        out[name + "_phase_s"] = {key: round(v, 4) for key, v in ctx.timings()["seconds"].items()}
         ctx.close()
     S0, U0 = res["plain_c128"][2], res["plain_c128"][0]
     k = wl.k

@@ -152,6 +152,66 @@ __global__ void __launch_bounds__(256) k_gram_part(const z128 *__restrict__ X, i
   }
 }
 
+// Gram partials of X with itself: only the K(K+1)/2 pairs a <= b are
+// computed (the lower triangle is written as their conjugates; the
+// Cholesky reads the upper one). With few pairs the block's threads split
+// into row groups (rows g, g + groups, ... of each staged tile) whose sums
+// are added in group order at the end, so that all threads have work.
+__global__ void __launch_bounds__(256) k_gram_sym(const z128 *__restrict__ X, int64_t sx, int64_t rows, int K,
+                                                  z128 *__restrict__ part) {
+  extern __shared__ z128 sm[];  // [kGramTile][K] rows, then [256] group sums
+  const int iw = blockIdx.y, nw = gridDim.y;
+  const int64_t n0 = (int64_t)blockIdx.x * kGramRows;
+  const int64_t n1 = min(rows, n0 + kGramRows);
+  const int P = K * (K + 1) / 2;
+  const int groups = P <= (int)blockDim.x ? (int)blockDim.x / P : 1;
+  z128 *tile = sm, *red = sm + kGramTile * K;
+  int g = 0, p;
+  if (groups > 1) {
+    g = threadIdx.x / P;
+    p = threadIdx.x - g * P;
+  } else {
+    p = blockIdx.z * blockDim.x + threadIdx.x;
+  }
+  const bool act = groups > 1 ? g < groups : p < P;
+  int a = 0, b = 0;
+  if (act) {
+    int rem = p;
+    while (rem >= K - a) {
+      rem -= K - a;
+      ++a;
+    }
+    b = a + rem;
+  }
+  z128 s = zmake<z128>(0, 0);
+  for (int64_t nb = n0; nb < n1; nb += kGramTile) {
+    const int nr = (int)min((int64_t)kGramTile, n1 - nb);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nr * K; e += blockDim.x) {
+      const int rr = e / K, c = e - rr * K;
+      tile[rr * K + c] = X[(nb + rr) * sx + (int64_t)iw * K + c];
+    }
+    __syncthreads();
+    if (act)
+      for (int rr = g; rr < nr; rr += groups) zmacc(s, tile[rr * K + a], tile[rr * K + b]);
+  }
+  z128 *out = part + ((int64_t)blockIdx.x * nw + iw) * K * K;
+  if (groups > 1) {
+    if (act) red[threadIdx.x] = s;
+    __syncthreads();
+    if (!act || g != 0) return;
+    for (int q = 1; q < groups; ++q) {
+      const z128 v = red[q * P + p];
+      s.re += v.re;
+      s.im += v.im;
+    }
+  } else if (!act) {
+    return;
+  }
+  out[a * K + b] = s;
+  if (b != a) out[b * K + a] = zmake<z128>(s.re, -s.im);
+}
+
 // G[iw][p] = sum over chunks (fixed order).
 __global__ void k_gram_reduce(const z128 *__restrict__ part, int chunks, int nw, int pairs,
                               z128 *__restrict__ G) {
@@ -255,6 +315,41 @@ __global__ void __launch_bounds__(256) k_apply_small(z128 *__restrict__ Y, int64
   Y[n * stride + (int64_t)iw * K + b] = s;
 }
 
+// Y[n][iw][:] <- Y[n][iw][:] * M[iw] for an upper-triangular M, in place.
+// Output b needs b + 1 products, so thread j of a row-frequency pair's
+// H = ceil(K/2) threads takes outputs j and K-1-j: K + 1 products each
+// (the warp's lanes finish together).
+__global__ void __launch_bounds__(256) k_apply_upper(z128 *__restrict__ Y, int64_t stride, int64_t rows, int nw,
+                                                     int K, const z128 *__restrict__ M) {
+  extern __shared__ z128 sm[];
+  const int H = (K + 1) / 2;
+  const int per = blockDim.x / H;
+  const int local = threadIdx.x / H, j = threadIdx.x - local * H;
+  const int64_t pairid = (int64_t)blockIdx.x * per + local;
+  const bool active = local < per && pairid < rows * nw;
+  int64_t n = 0;
+  int iw = 0;
+  if (active) {
+    n = pairid / nw;
+    iw = (int)(pairid - n * nw);
+    const z128 *y = Y + n * stride + (int64_t)iw * K;
+    sm[local * K + j] = y[j];
+    if (K - 1 - j != j) sm[local * K + K - 1 - j] = y[K - 1 - j];
+  }
+  __syncthreads();
+  if (!active) return;
+  const z128 *m = M + (int64_t)iw * K * K;
+  const z128 *x = sm + local * K;
+  z128 s1 = zmake<z128>(0, 0), s2 = zmake<z128>(0, 0);
+  const int b1 = j, b2 = K - 1 - j;
+  for (int a = 0; a <= b1; ++a) zmac(s1, x[a], m[a * K + b1]);
+  if (b2 != b1)
+    for (int a = 0; a <= b2; ++a) zmac(s2, x[a], m[a * K + b2]);
+  z128 *y = Y + n * stride + (int64_t)iw * K;
+  y[b1] = s1;
+  if (b2 != b1) y[b2] = s2;
+}
+
 struct DenseScratch {
   z128 *part, *G, *R, *Rinv, *Racc;
   int chunks;
@@ -286,9 +381,15 @@ static rsvdt_status gram(rsvdt_ctx *ctx, const z128 *X, int64_t sx, const z128 *
                          int64_t rows, int nw, int KA, int KB, DenseScratch &s) {
   if (KA + KB > 256) return set_err(ctx, RSVDT_ERR_ARG, "block too wide for the Gram kernel (%d x %d)", KA, KB);
   const int pairs_ = KA * KB;
-  dim3 g(s.chunks, nw, (pairs_ + 1023) / 1024);
-  size_t sm = sizeof(z128) * kGramTile * (KA + KB);
-  k_gram_part<<<g, 256, sm, ctx->stream>>>(X, sx, Y, sy, rows, KA, KB, s.part);
+  if (X == Y && sx == sy && KA == KB) {
+    const int P = KA * (KA + 1) / 2;
+    dim3 g(s.chunks, nw, P <= 256 ? 1 : (P + 255) / 256);
+    k_gram_sym<<<g, 256, sizeof(z128) * (kGramTile * KA + 256), ctx->stream>>>(X, sx, rows, KA, s.part);
+  } else {
+    dim3 g(s.chunks, nw, (pairs_ + 1023) / 1024);
+    size_t sm = sizeof(z128) * kGramTile * (KA + KB);
+    k_gram_part<<<g, 256, sm, ctx->stream>>>(X, sx, Y, sy, rows, KA, KB, s.part);
+  }
   const int pairs = KA * KB;
   k_gram_reduce<<<grid_for((int64_t)nw * pairs, 256), 256, 0, ctx->stream>>>(s.part, s.chunks, nw,
                                                                               pairs, s.G);
@@ -299,10 +400,15 @@ static rsvdt_status gram(rsvdt_ctx *ctx, const z128 *X, int64_t sx, const z128 *
 static rsvdt_status apply_small(rsvdt_ctx *ctx, z128 *Y, int64_t stride, int64_t rows, int nw,
                                 int K, const z128 *M, bool upper) {
   if (K > 256) return set_err(ctx, RSVDT_ERR_ARG, "block too wide (%d)", K);
-  const int per = 256 / K;
   const int64_t pairs = rows * nw;
-  k_apply_small<<<grid_for(pairs, per), per * K, sizeof(z128) * per * K, ctx->stream>>>(
-      Y, stride, rows, nw, K, M, upper ? 1 : 0);
+  if (upper) {
+    const int H = (K + 1) / 2, per = 256 / H;
+    k_apply_upper<<<grid_for(pairs, per), per * H, sizeof(z128) * per * K, ctx->stream>>>(Y, stride, rows, nw, K, M);
+  } else {
+    const int per = 256 / K;
+    k_apply_small<<<grid_for(pairs, per), per * K, sizeof(z128) * per * K, ctx->stream>>>(Y, stride, rows, nw, K,
+                                                                                       M, 0);
+  }
   ctx->launches += 1;
   return cuda_ok(ctx, cudaGetLastError(), "apply") ? RSVDT_OK : RSVDT_ERR_CUDA;
 }
