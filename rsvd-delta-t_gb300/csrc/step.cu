@@ -1108,11 +1108,86 @@ __global__ void __launch_bounds__(256) k_dft(const Z *__restrict__ ring,
   out[(n * Nwe + iw) * Kb + k0 + kc] = s;
 }
 
+// The same DFT by a radix-2 FFT when Nw is a power of two (NW = 8, 16, 32):
+// one thread per (row, test vector) holds the NW samples in registers
+// (loaded in bit-reversed order), NW/2 log2(NW) butterflies with the
+// twiddles W^m = dft[1][m] of the reference's own table
+// (SourceCode/CreateDFTiDFTMats.c:61-85), FP64 arithmetic: NW/2 log2(NW)
+// complex products per output set instead of NW * Nw_eff. The first Nw_eff
+// outputs are kept (all of them for a complex operator).
+__device__ __forceinline__ constexpr int bit_reverse(int p, int bits) {
+  int r = 0;
+  for (int b = 0; b < bits; ++b) r |= ((p >> b) & 1) << (bits - 1 - b);
+  return r;
+}
+
+template <class Z, int NW, int LOG>
+__global__ void __launch_bounds__(128) k_dft_fft(const Z *__restrict__ ring, const z128 *__restrict__ dft,
+                                                 int64_t N, int K, int Nwe, double R, z128 *__restrict__ out,
+                                                 int32_t *flags, int Kb, int k0) {
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u >= N * K) return;
+  const int64_t n = u / K;
+  const int kc = (int)(u - n * K);
+  const int64_t NK = N * K;
+  double re[NW], im[NW];
+#pragma unroll
+  for (int p = 0; p < NW; ++p) {
+    const Z v = ring[(int64_t)p * NK + u];
+    re[bit_reverse(p, LOG)] = (double)v.re;
+    im[bit_reverse(p, LOG)] = (double)v.im;
+  }
+#pragma unroll
+  for (int half = 1; half < NW; half <<= 1) {
+#pragma unroll
+    for (int j = 0; j < half; ++j) {
+      const double2 wt = __ldg(reinterpret_cast<const double2 *>(dft) + NW + j * (NW / (2 * half)));
+      const z128 w = zmake<z128>(wt.x, wt.y);
+#pragma unroll
+      for (int i = j; i < NW; i += 2 * half) {
+        const double xr = re[i + half], xi = im[i + half];
+        const double tr = fma(w.re, xr, -w.im * xi), ti = fma(w.re, xi, w.im * xr);
+        re[i + half] = re[i] - tr;
+        im[i + half] = im[i] - ti;
+        re[i] += tr;
+        im[i] += ti;
+      }
+    }
+  }
+  bool ok = true;
+#pragma unroll
+  for (int iw = 0; iw < NW; ++iw) {
+    if (iw < Nwe) {
+      const z128 s = zmake<z128>(re[iw] * R, im[iw] * R);
+      ok = ok && isfinite(s.re) && isfinite(s.im);
+      out[(n * Nwe + iw) * Kb + k0 + kc] = s;
+    }
+  }
+  if (!ok) atomicOr(flags, 1);
+}
+
+template <class Z>
+static bool launch_dft_fft(rsvdt_ctx *ctx, const Z *ring, z128 *out) {
+  const int64_t total = ctx->N * ctx->Ks;
+  const int g = grid_for(total, 128);
+  const int K = (int)ctx->Ks, Nwe = (int)ctx->Nw_eff, Kb = (int)ctx->K, k0 = (int)ctx->k0;
+  const double R = (double)ctx->R;
+  switch (ctx->Nw) {
+    case 8: k_dft_fft<Z, 8, 3><<<g, 128, 0, ctx->stream>>>(ring, ctx->dft, ctx->N, K, Nwe, R, out, ctx->d_flags, Kb, k0); return true;
+    case 16: k_dft_fft<Z, 16, 4><<<g, 128, 0, ctx->stream>>>(ring, ctx->dft, ctx->N, K, Nwe, R, out, ctx->d_flags, Kb, k0); return true;
+    case 32: k_dft_fft<Z, 32, 5><<<g, 128, 0, ctx->stream>>>(ring, ctx->dft, ctx->N, K, Nwe, R, out, ctx->d_flags, Kb, k0); return true;
+    default: return false;
+  }
+}
+
 // DFT of the ring (the state's Ks test vectors) into columns k0.. of `out`.
 rsvdt_status launch_dft(rsvdt_ctx *ctx, int prec, z128 *out) {
   const int th = 256;
   const int64_t total = ctx->N * ctx->Nw_eff * ctx->Ks;
-  if (prec == RSVDT_PREC_C64)
+  const bool fft = prec == RSVDT_PREC_C64 ? launch_dft_fft<z64>(ctx, (const z64 *)ctx->ring, out)
+                                          : launch_dft_fft<z128>(ctx, (const z128 *)ctx->ring, out);
+  if (fft) {
+  } else if (prec == RSVDT_PREC_C64)
     k_dft<z64><<<grid_for(total, th), th, 0, ctx->stream>>>(
         (const z64 *)ctx->ring, ctx->dft, ctx->N, (int)ctx->Ks, (int)ctx->Nw, (int)ctx->Nw_eff,
         (double)ctx->R, out, ctx->d_flags, (int)ctx->K, (int)ctx->k0);
