@@ -1108,7 +1108,7 @@ __global__ void __launch_bounds__(256) k_dft(const Z *__restrict__ ring,
   out[(n * Nwe + iw) * Kb + k0 + kc] = s;
 }
 
-// The same DFT by a radix-2 FFT when Nw is a power of two (NW = 8, 16, 32):
+// The same DFT by a radix-2 FFT when Nw is 8, 16, 32 (64: k_dft_fft64):
 // one thread per (row, test vector) holds the NW samples in registers
 // (loaded in bit-reversed order), NW/2 log2(NW) butterflies with the
 // twiddles W^m = dft[1][m] of the reference's own table
@@ -1166,6 +1166,71 @@ __global__ void __launch_bounds__(128) k_dft_fft(const Z *__restrict__ ring, con
   if (!ok) atomicOr(flags, 1);
 }
 
+// Nw = 64: two lanes per (row, test vector). Lane h transforms the samples
+// p = 2m + h (a 32-point FFT, twiddles W64^(2j)); the pair then exchanges
+// one value per output through a shuffle: X[k] = E[k] + W64^k O[k] (lane 0),
+// X[k + 32] = E[k] - W64^k O[k] (lane 1).
+template <class Z>
+__global__ void __launch_bounds__(128) k_dft_fft64(const Z *__restrict__ ring, const z128 *__restrict__ dft,
+                                                   int64_t N, int K, int Nwe, double R, z128 *__restrict__ out,
+                                                   int32_t *flags, int Kb, int k0) {
+  constexpr int NW = 64, H = 32, LOG = 5;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t u = t >> 1;
+  const int h = (int)(t & 1);
+  const bool valid = u < N * K;  // both lanes of a pair agree
+  const int64_t uu = valid ? u : 0;
+  const int64_t n = uu / K;
+  const int kc = (int)(uu - n * K);
+  const int64_t NK = N * K;
+  double re[H], im[H];
+#pragma unroll
+  for (int m = 0; m < H; ++m) {
+    double vr = 0, vi = 0;
+    if (valid) {
+      const Z v = ring[(int64_t)(2 * m + h) * NK + uu];
+      vr = (double)v.re;
+      vi = (double)v.im;
+    }
+    re[bit_reverse(m, LOG)] = vr;
+    im[bit_reverse(m, LOG)] = vi;
+  }
+  const double2 *tw = reinterpret_cast<const double2 *>(dft) + NW;  // W64^m = dft[1][m]
+#pragma unroll
+  for (int half = 1; half < H; half <<= 1) {
+#pragma unroll
+    for (int j = 0; j < half; ++j) {
+      const double2 w = __ldg(tw + 2 * j * (H / (2 * half)));
+#pragma unroll
+      for (int i = j; i < H; i += 2 * half) {
+        const double xr = re[i + half], xi = im[i + half];
+        const double tr = fma(w.x, xr, -w.y * xi), ti = fma(w.x, xi, w.y * xr);
+        re[i + half] = re[i] - tr;
+        im[i + half] = im[i] - ti;
+        re[i] += tr;
+        im[i] += ti;
+      }
+    }
+  }
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < H; ++k) {
+    const double pr = __shfl_xor_sync(0xffffffffu, re[k], 1), pi = __shfl_xor_sync(0xffffffffu, im[k], 1);
+    // Lane 0 holds E[k] and receives O[k]; lane 1 holds O[k] and receives E[k].
+    const double er = h ? pr : re[k], ei = h ? pi : im[k];
+    const double orr = h ? re[k] : pr, oi = h ? im[k] : pi;
+    const double2 w = __ldg(tw + k);
+    const double tr = fma(w.x, orr, -w.y * oi), ti = fma(w.x, oi, w.y * orr);
+    const int iw = k + h * H;
+    if (valid && iw < Nwe) {
+      const z128 s = zmake<z128>((h ? er - tr : er + tr) * R, (h ? ei - ti : ei + ti) * R);
+      ok = ok && isfinite(s.re) && isfinite(s.im);
+      out[(n * Nwe + iw) * Kb + k0 + kc] = s;
+    }
+  }
+  if (!ok) atomicOr(flags, 1);
+}
+
 template <class Z>
 static bool launch_dft_fft(rsvdt_ctx *ctx, const Z *ring, z128 *out) {
   const int64_t total = ctx->N * ctx->Ks;
@@ -1176,6 +1241,10 @@ static bool launch_dft_fft(rsvdt_ctx *ctx, const Z *ring, z128 *out) {
     case 8: k_dft_fft<Z, 8, 3><<<g, 128, 0, ctx->stream>>>(ring, ctx->dft, ctx->N, K, Nwe, R, out, ctx->d_flags, Kb, k0); return true;
     case 16: k_dft_fft<Z, 16, 4><<<g, 128, 0, ctx->stream>>>(ring, ctx->dft, ctx->N, K, Nwe, R, out, ctx->d_flags, Kb, k0); return true;
     case 32: k_dft_fft<Z, 32, 5><<<g, 128, 0, ctx->stream>>>(ring, ctx->dft, ctx->N, K, Nwe, R, out, ctx->d_flags, Kb, k0); return true;
+    case 64:
+      k_dft_fft64<Z><<<grid_for(2 * total, 128), 128, 0, ctx->stream>>>(ring, ctx->dft, ctx->N, K, Nwe, R, out,
+                                                                       ctx->d_flags, Kb, k0);
+      return true;
     default: return false;
   }
 }
