@@ -473,6 +473,16 @@ def learned3d_form(n: int = 48, n_train: int = 24, n_held: int = 8, seed: int = 
     return out
 
 
+def step_config(wl, dt, Ns, R, step_bytes, world):
+    """The benchmark step's `config` (both arms)."""
+    return {"workload": f"{wl.name}: one forced RK4 step over k={wl.k} test vectors of the five-field "
+                        f"{wl.meta['grid']} block operator (5x5 blocks), Nw={wl.Nw}, "
+                        "complex128",
+            "N": wl.N, "nnz": wl.meta["nnz"], "k": wl.k, "Nw": wl.Nw, "dt": dt, "Ns": Ns, "ResRatio": R,
+            "step_bytes": step_bytes, "l2": "working set 14 GB >> L2, no flush", "parallelism": f"replicas x{world}",
+            "spectral_shift": round(wl.meta["shift"], 6), "shift_method": wl.meta["shift_method"]}
+
+
 def run_reference(args):
     """CPU arm: the reference algorithm on the host cores (oracle port)."""
     rank = int(os.environ.get("RANK", "0"))
@@ -494,8 +504,7 @@ def run_reference(args):
     out = {"impl": "reference", "metric": METRIC, "value": round(val, 3), "unit": "GB/s", "n_gpus": args.gpus,
            "steps": max(1, min(args.steps, 3)), "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-           "config": {"workload": f"{wl.name} five-field block operator, k={wl.k}, Nw={wl.Nw}, one forced RK4 step",
-                      "N": wl.N, "nnz": wl.meta["nnz"], "k": wl.k, "Nw": wl.Nw},
+           "config": step_config(wl, dt, Ns, R, b["step"], args.gpus),
            "cpu_baseline": {"value": round(val, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                             "sample": f"{max(1, min(args.steps, 3))} steps x {wl.k} test vectors, row loops on "
                                       f"{threads} threads; C restatement of SourceCode/TSRK4.c (PETSc/SLEPc/MPI "
@@ -651,12 +660,7 @@ def main():
             "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded operator and sketch)",
-            "config": {"workload": f"{wl.name}: one forced RK4 step over k={wl.k} test vectors of the five-field "
-                                   f"64^3 block operator (5x5 blocks), Nw={wl.Nw}, complex128",
-                       "N": wl.N, "nnz": wl.meta["nnz"], "k": wl.k, "Nw": wl.Nw, "dt": g.dt, "Ns": g.Ns,
-                       "ResRatio": g.ResRatio, "step_bytes": b["step"], "l2": "working set 14 GB >> L2, no flush",
-                       "parallelism": f"replicas x{world}",
-                       "spectral_shift": round(wl.meta["shift"], 6), "shift_method": wl.meta["shift_method"]},
+            "config": step_config(wl, g.dt, g.Ns, g.ResRatio, b["step"], world),
             "roofline": {"bound": "hbm", "kernel": "k_rstage<z128,10,1> (block-row SpMM + forcing synthesis)",
                          "achieved": round(ach, 2), "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4),
                          "peak_kind": peak_kind,
