@@ -1429,6 +1429,26 @@ __global__ void __launch_bounds__(256) k_stage_batched(const StepArgs<Z> *__rest
     if (S == 4) step[0] = i + 1;
   }
   if (i > P.rend) return;  // uniform over the block (one problem per block)
+  // Stage 1: the step's two phasor rows in shared memory (read once per
+  // slab by every thread of the block).
+  constexpr int kMaxStagedNw = 128;
+  __shared__ Z e_sm[S == 1 ? 2 * kMaxStagedNw : 1];
+  const Z *e2 = nullptr, *e3 = nullptr;
+  if (S == 1 && P.Fh) {
+    int64_t j2, j3;
+    step_idx(P.dir, i, P.two_ns, j2, j3);
+    e2 = P.tab + j2 * P.Nw;
+    e3 = P.tab + j3 * P.Nw;
+    if (P.Nw <= kMaxStagedNw) {
+      for (int s = threadIdx.x; s < P.Nw; s += blockDim.x) {
+        e_sm[s] = e2[s];
+        e_sm[kMaxStagedNw + s] = e3[s];
+      }
+      __syncthreads();
+      e2 = e_sm;
+      e3 = e_sm + kMaxStagedNw;
+    }
+  }
   const int64_t local = (int64_t)wk.y * blockDim.x + threadIdx.x;
   const int64_t u = local / FS;
   const int fsub = (int)(local - u * FS);
@@ -1440,11 +1460,7 @@ __global__ void __launch_bounds__(256) k_stage_batched(const StepArgs<Z> *__rest
   Z k = zmake<Z>(0, 0), f2 = zmake<Z>(0, 0), f3 = zmake<Z>(0, 0);
   if (valid) {
     row_product_split(P, n, kc, x, k, fsub, FS);
-    if (S == 1 && P.Fh) {
-      int64_t j2, j3;
-      step_idx(P.dir, i, P.two_ns, j2, j3);
-      forcing2(P, n, kc, P.tab + j2 * P.Nw, P.tab + j3 * P.Nw, fsub, FS, f2, f3);
-    }
+    if (S == 1 && P.Fh) forcing2(P, n, kc, e2, e3, fsub, FS, f2, f3);
   }
   if (FS > 1) {
     group_sum<Z, FS>(k);
