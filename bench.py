@@ -266,7 +266,8 @@ def batch_form(count: int = 48, q: int = 0, seed: int = 2024):
                                         "beta": round(fam[worst]["beta"], 4),
                                         "sigma1_max": float(S_seq[worst][0].max()),
                                         "problems_over_1e-3": int(sum(e > 1e-3 for e in errs))}
-        out[name + "_tuned"] = {"threads": th, "lanes_per_row": lanes, "ms_per_batched_step": round(ms, 4)}
+        out[name + "_tuned"] = {"threads": th, "lanes_per_row": lanes, "values_per_lane": b.values_per_lane(),
+                                "ms_per_batched_step": round(ms, 4)}
         b.close()
     return out
 

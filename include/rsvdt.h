@@ -346,6 +346,14 @@ rsvdt_status rsvdt_batch_get_grid(const rsvdt_batch *b, int32_t index, rsvdt_gri
 /* Launch shape chosen by the autotuner and its time per batched step. */
 rsvdt_status rsvdt_batch_get_tuning(const rsvdt_batch *b, int32_t *threads, int32_t *lanes_per_row,
                                     double *ms_per_step);
+/* Test vectors per lane of the chosen shape: 1, or 2 (complex64 stages,
+ * every problem's k even: 16-byte accesses). */
+int32_t rsvdt_batch_values_per_lane(const rsvdt_batch *b);
+/* Fixes the launch shape instead of autotuning it (threads 128 or 256,
+ * lanes per row 1/2/4/8, values per lane 1 or 2); threads = 0 returns to
+ * the autotuner. Call after the last rsvdt_batch_add. */
+rsvdt_status rsvdt_batch_set_launch_shape(rsvdt_batch *b, int32_t threads, int32_t lanes_per_row,
+                                          int32_t values_per_lane);
 int64_t rsvdt_batch_launch_count(const rsvdt_batch *b);
 
 /* ------------------------------------------------------- learned sketch

@@ -33,7 +33,11 @@ struct rsvdt_batch {
   std::vector<unsigned char> h_args;
   int2 *d_work = nullptr;
   int nwork = 0;
-  int threads = 0, fs = 0;
+  // With two values per lane, the one-value list of the same shape for the
+  // refinement form's complex128 action.
+  int2 *d_work1 = nullptr;
+  int nwork1 = 0;
+  int threads = 0, fs = 0, kv = 1;  // launch shape: threads, lanes per value, values per lane
   double tuned_ms = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   cudaGraphExec_t graph128[2] = {nullptr, nullptr};
@@ -77,21 +81,27 @@ static void free_batch_graphs(rsvdt_batch *b) {
 static void **args_for(rsvdt_batch *b, int prec) { return prec == b->prec ? b->d_args : b->d_args128; }
 static cudaGraphExec_t *graphs_for(rsvdt_batch *b, int prec) { return prec == b->prec ? b->graph : b->graph128; }
 
-// Work list (problem, tile) for a launch shape.
-static rsvdt_status build_work(rsvdt_batch *b, int threads, int fs) {
+// Work list (problem, tile) for a launch shape into *dst / *n.
+static rsvdt_status build_list(rsvdt_batch *b, int threads, int fs, int kv, int2 **dst, int *n) {
   std::vector<int2> w;
   for (size_t p = 0; p < b->probs.size(); ++p) {
-    const int64_t nk = b->probs[p]->N * b->probs[p]->K * fs;
+    const int64_t nk = b->probs[p]->N * b->probs[p]->K * fs / kv;
     const int64_t tiles = (nk + threads - 1) / threads;
     for (int64_t t = 0; t < tiles; ++t) w.push_back(make_int2((int)p, (int)t));
   }
-  if (b->d_work) cudaFree(b->d_work);
-  b->d_work = nullptr;
-  if (!bcuda(b, cudaMalloc(&b->d_work, sizeof(int2) * std::max<size_t>(w.size(), 1)), "work list")) return RSVDT_ERR_OOM;
-  if (!bcuda(b, cudaMemcpy(b->d_work, w.data(), sizeof(int2) * w.size(), cudaMemcpyHostToDevice), "work list"))
+  if (*dst) cudaFree(*dst);
+  *dst = nullptr;
+  if (!bcuda(b, cudaMalloc(dst, sizeof(int2) * std::max<size_t>(w.size(), 1)), "work list")) return RSVDT_ERR_OOM;
+  if (!bcuda(b, cudaMemcpy(*dst, w.data(), sizeof(int2) * w.size(), cudaMemcpyHostToDevice), "work list"))
     return RSVDT_ERR_CUDA;
-  b->nwork = (int)w.size();
+  *n = (int)w.size();
   return RSVDT_OK;
+}
+
+static rsvdt_status build_work(rsvdt_batch *b, int threads, int fs, int kv) {
+  rsvdt_status st = build_list(b, threads, fs, kv, &b->d_work, &b->nwork);
+  if (st || kv == 1 || !b->refine) return st;
+  return build_list(b, threads, fs, 1, &b->d_work1, &b->nwork1);
 }
 
 // Argument blocks of every problem for direction d; rend[p] = 0 leaves a
@@ -113,8 +123,11 @@ static rsvdt_status capture(rsvdt_batch *b, int d, int prec) {
   cudaGraph_t g;
   if (!bcuda(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture"))
     return RSVDT_ERR_CUDA;
+  // The refinement form's complex128 action takes one value per lane.
+  const bool own = prec == b->prec || b->kv == 1;
   for (int s = 0; s < kBatchGraphSteps; ++s)
-    launch_batched_step(b->stream, prec, args_for(b, prec)[d], b->d_work, b->nwork, b->threads, b->fs, b->d_step);
+    launch_batched_step(b->stream, prec, args_for(b, prec)[d], own ? b->d_work : b->d_work1,
+                        own ? b->nwork : b->nwork1, b->threads, b->fs, b->d_step, prec == b->prec ? b->kv : 1);
   if (!bcuda(b, cudaStreamEndCapture(b->stream, &g), "end capture")) return RSVDT_ERR_CUDA;
   const cudaError_t e = cudaGraphInstantiate(&graphs_for(b, prec)[d], g, 0);
   cudaGraphDestroy(g);
@@ -127,22 +140,28 @@ static rsvdt_status capture(rsvdt_batch *b, int d, int prec) {
 // caller afterwards.
 static rsvdt_status autotune(rsvdt_batch *b, int d) {
   static const int cand_threads[] = {128, 256};
-  static const int cand_fs[] = {1, 2, 4, 8};
+  // (lanes per value, values per lane); two values per lane only for
+  // complex64 stages with every problem's k even.
+  static const int cand_shape[][2] = {{1, 1}, {2, 1}, {4, 1}, {8, 1}, {1, 2}};
+  bool even_k = true;
+  for (auto *c : b->probs) even_k = even_k && c->K % 2 == 0;
   const int steps = 8;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   double best = 1e30;
-  int bt = 0, bf = 0;
+  int bt = 0, bf = 0, bk = 1;
   for (int th : cand_threads)
-    for (int fs : cand_fs) {
-      rsvdt_status st = build_work(b, th, fs);
+    for (const auto &shape : cand_shape) {
+      const int fs = shape[0], kv = shape[1];
+      if (kv == 2 && (b->prec != RSVDT_PREC_C64 || !even_k)) continue;
+      rsvdt_status st = build_work(b, th, fs, kv);
       if (st) return st;
       for (int rep = 0; rep < 2; ++rep) {  // first repetition warms up
         launch_set_step(b->stream, b->d_step, 1);
         cudaEventRecord(e0, b->stream);
         for (int s = 0; s < steps; ++s)
-          launch_batched_step(b->stream, b->prec, b->d_args[d], b->d_work, b->nwork, th, fs, b->d_step);
+          launch_batched_step(b->stream, b->prec, b->d_args[d], b->d_work, b->nwork, th, fs, b->d_step, kv);
         cudaEventRecord(e1, b->stream);
         if (!bcuda(b, cudaEventSynchronize(e1), "autotune")) return RSVDT_ERR_CUDA;
       }
@@ -152,14 +171,16 @@ static rsvdt_status autotune(rsvdt_batch *b, int d) {
         best = ms / steps;
         bt = th;
         bf = fs;
+        bk = kv;
       }
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   b->threads = bt;
   b->fs = bf;
+  b->kv = bk;
   b->tuned_ms = best;
-  return build_work(b, bt, bf);
+  return build_work(b, bt, bf, bk);
 }
 
 // One action (direct d = 1 or adjoint d = 0) of every problem in `mask`,
@@ -228,6 +249,7 @@ void rsvdt_batch_destroy(rsvdt_batch *b) {
   for (auto p : b->d_args128)
     if (p) cudaFree(p);
   if (b->d_work) cudaFree(b->d_work);
+  if (b->d_work1) cudaFree(b->d_work1);
   if (b->d_step) cudaFree(b->d_step);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -296,7 +318,7 @@ rsvdt_status rsvdt_batch_run(rsvdt_batch *b) {
         return RSVDT_ERR_OOM;
     }
     if (b->threads) {
-      rsvdt_status st = build_work(b, b->threads, b->fs);
+      rsvdt_status st = build_work(b, b->threads, b->fs, b->kv);
       if (st) return st;
     }
     b->ready = true;
@@ -342,6 +364,35 @@ rsvdt_status rsvdt_batch_get_tuning(const rsvdt_batch *b, int32_t *threads, int3
   if (threads) *threads = b->threads;
   if (lanes_per_row) *lanes_per_row = b->fs;
   if (ms_per_step) *ms_per_step = b->tuned_ms;
+  return RSVDT_OK;
+}
+
+int32_t rsvdt_batch_values_per_lane(const rsvdt_batch *b) { return b ? b->kv : 0; }
+
+rsvdt_status rsvdt_batch_set_launch_shape(rsvdt_batch *b, int32_t threads, int32_t lanes_per_row,
+                                          int32_t values_per_lane) {
+  if (!b) return RSVDT_ERR_ARG;
+  if (threads == 0) {  // back to the autotuner
+    b->threads = 0;
+    b->fs = 0;
+    b->kv = 1;
+    free_batch_graphs(b);
+    return RSVDT_OK;
+  }
+  if ((threads != 128 && threads != 256) ||
+      (lanes_per_row != 1 && lanes_per_row != 2 && lanes_per_row != 4 && lanes_per_row != 8) ||
+      (values_per_lane != 1 && values_per_lane != 2))
+    return bfail(b, RSVDT_ERR_ARG, "launch shape: threads 128 or 256, lanes per row 1, 2, 4 or 8, values per lane 1 or 2");
+  if (values_per_lane == 2 && (b->prec != RSVDT_PREC_C64 || lanes_per_row != 1))
+    return bfail(b, RSVDT_ERR_ARG, "two values per lane need complex64 stages and one lane per row");
+  for (auto *c : b->probs)
+    if (values_per_lane == 2 && c->K % 2)
+      return bfail(b, RSVDT_ERR_ARG, "two values per lane need an even k in every problem");
+  b->threads = threads;
+  b->fs = lanes_per_row;
+  b->kv = values_per_lane;
+  free_batch_graphs(b);
+  b->ready = false;  // rebuild the work lists
   return RSVDT_OK;
 }
 

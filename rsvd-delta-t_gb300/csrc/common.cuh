@@ -259,7 +259,7 @@ rsvdt_status launch_dft(rsvdt_ctx *ctx, int prec, z128 *out);
 size_t step_args_size(int prec);
 void fill_step_args(rsvdt_ctx *ctx, int dir, int prec, int64_t rend, int64_t *shared_step, void *out);
 bool launch_batched_step(cudaStream_t st, int prec, const void *args, const int2 *work, int nwork, int threads,
-                         int fs, int64_t *step);
+                         int fs, int64_t *step, int kv = 1);
 void launch_set_step(cudaStream_t st, int64_t *step, int64_t i);
 rsvdt_status launch_unforced_steps(rsvdt_ctx *ctx, int dir, z128 *cols, int64_t ncols,
                                    int64_t nsteps);

@@ -1494,6 +1494,162 @@ __global__ void __launch_bounds__(256) k_stage_batched(const StepArgs<Z> *__rest
   }
 }
 
+// complex64 batched stage with two test vectors per lane (every problem of
+// the batch has an even k): a lane owns (row n, test vectors kc, kc+1), so
+// every state, slab and gathered access is one 16-byte load or store
+// instead of two 8-byte ones. Each of the two values is computed exactly as
+// k_stage_batched<z64, S, 1> computes it (the same operations in the same
+// order: bit-identical results).
+template <int S>
+__global__ void __launch_bounds__(256) k_stage_batched_pair(const StepArgs<z64> *__restrict__ probs,
+                                                            const int2 *__restrict__ work, int64_t *step) {
+  using Z = z64;
+  pdl_wait_and_release();
+  const int2 wk = work[blockIdx.x];
+  const StepArgs<Z> &P = probs[wk.x];
+  const int64_t i = (S == 1) ? step[0] : step[1];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (S == 1) step[1] = i;
+    if (S == 4) step[0] = i + 1;
+  }
+  if (i > P.rend) return;  // uniform over the block (one problem per block)
+  constexpr int kMaxStagedNw = 128;
+  __shared__ Z e_sm[S == 1 ? 2 * kMaxStagedNw : 1];
+  const Z *e2 = nullptr, *e3 = nullptr;
+  if (S == 1 && P.Fh) {
+    int64_t j2, j3;
+    step_idx(P.dir, i, P.two_ns, j2, j3);
+    e2 = P.tab + j2 * P.Nw;
+    e3 = P.tab + j3 * P.Nw;
+    if (P.Nw <= kMaxStagedNw) {
+      for (int s = threadIdx.x; s < P.Nw; s += blockDim.x) {
+        e_sm[s] = e2[s];
+        e_sm[kMaxStagedNw + s] = e3[s];
+      }
+      __syncthreads();
+      e2 = e_sm;
+      e3 = e_sm + kMaxStagedNw;
+    }
+  }
+  const int64_t NK = P.N * P.K;
+  const int64_t t = 2 * ((int64_t)wk.y * blockDim.x + threadIdx.x);  // first of the lane's two values
+  if (t >= NK) return;
+  const int K = P.K;
+  const int64_t n = t / K;
+  const int kc = (int)(t - n * K);
+  const Z *x = (S == 1) ? P.y : (S == 2) ? P.zA : (S == 3) ? P.zB : P.zA;
+  Z k[2] = {zmake<Z>(0, 0), zmake<Z>(0, 0)};
+  if (P.bs == 0) {
+    const int32_t b = __ldg(P.rowptr + n), e = __ldg(P.rowptr + n + 1);
+    for (int32_t j = b; j < e; ++j) {
+      const int32_t cj = __ldg(P.col + j);
+      if (!RSVDT_CHECK_INDEX(cj >= 0 && cj < P.N, 0)) continue;
+      const Z a = P.val[j];
+      Z xv[2];
+      ld_chunk<Z, 2>(x + (int64_t)cj * K + kc, xv);
+      zmac(k[0], a, xv[0]);
+      zmac(k[1], a, xv[1]);
+    }
+  } else {
+    const int bs = P.bs;
+    const int64_t br = n / bs;
+    const int r = (int)(n - br * bs);
+    const int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
+    for (int32_t j = b; j < e; ++j) {
+      const int32_t cb = __ldg(P.col + j);
+      if (!RSVDT_CHECK_INDEX(cb >= 0 && cb < P.N / bs, 1)) continue;
+      const int64_t c0 = (int64_t)cb * bs;
+      const Z *blkrow = P.val + (int64_t)j * P.bstride + r * bs;
+      for (int c = 0; c < bs; ++c) {
+        Z xv[2];
+        ld_chunk<Z, 2>(x + (c0 + c) * K + kc, xv);
+        zmac(k[0], blkrow[c], xv[0]);
+        zmac(k[1], blkrow[c], xv[1]);
+      }
+    }
+  }
+  Z f2[2] = {zmake<Z>(0, 0), zmake<Z>(0, 0)}, f3[2] = {zmake<Z>(0, 0), zmake<Z>(0, 0)};
+  if (S == 1 && P.Fh) {
+    const Z *c = P.Fh + t;
+    if (!P.pair) {
+#pragma unroll 4
+      for (int s = 0; s < P.Nw; ++s) {
+        Z v[2];
+        ldg_chunk<Z, 2>(c + (int64_t)s * NK, v);
+        for (int q = 0; q < 2; ++q) {
+          zmac(f2[q], v[q], e2[s]);
+          zmac(f3[q], v[q], e3[s]);
+        }
+      }
+    } else {
+      const int H = P.Nw / 2, last = P.Nw - 1;
+      Z v[2];
+      ldg_chunk<Z, 2>(c, v);
+      for (int q = 0; q < 2; ++q) {
+        zmac(f2[q], v[q], e2[0]);
+        zmac(f3[q], v[q], e3[0]);
+      }
+      int s = 1;
+#pragma unroll 4
+      for (; s < H; ++s) {
+        ldg_chunk<Z, 2>(c + (int64_t)s * NK, v);
+        const auto w2 = e2[s].re, w3 = e3[s].re;
+        for (int q = 0; q < 2; ++q) {
+          f2[q].re = fma(w2, v[q].re, f2[q].re);
+          f2[q].im = fma(w2, v[q].im, f2[q].im);
+          f3[q].re = fma(w3, v[q].re, f3[q].re);
+          f3[q].im = fma(w3, v[q].im, f3[q].im);
+        }
+      }
+#pragma unroll 4
+      for (; s < last; ++s) {
+        ldg_chunk<Z, 2>(c + (int64_t)s * NK, v);
+        const auto w2 = e2[s - H + 1].im, w3 = e3[s - H + 1].im;
+        for (int q = 0; q < 2; ++q) {
+          f2[q].re = fma(w2, v[q].re, f2[q].re);
+          f2[q].im = fma(w2, v[q].im, f2[q].im);
+          f3[q].re = fma(w3, v[q].re, f3[q].re);
+          f3[q].im = fma(w3, v[q].im, f3[q].im);
+        }
+      }
+      ldg_chunk<Z, 2>(c + (int64_t)last * NK, v);
+      for (int q = 0; q < 2; ++q) {
+        zmac(f2[q], v[q], e2[H]);
+        zmac(f3[q], v[q], e3[H]);
+      }
+    }
+  }
+  Z addv[2], yv[2], t2[2];
+  ld_chunk<Z, 2>(((S == 1 || S == 4) ? P.F3 : P.F2) + t, addv);
+  for (int q = 0; q < 2; ++q) {
+    k[q].re += addv[q].re;
+    k[q].im += addv[q].im;
+  }
+  ld_chunk<Z, 2>(P.y + t, yv);
+  if (S == 1) {
+    st_chunk<Z, 2>(P.F2 + t, f2);
+    st_chunk<Z, 2>(P.F3 + t, f3);
+    for (int q = 0; q < 2; ++q) t2[q] = zaxpy(P.dt_2, k[q], yv[q]);
+    st_chunk<Z, 2>(P.zA + t, t2);
+    for (int q = 0; q < 2; ++q) t2[q] = zaxpy(P.dt_6, k[q], yv[q]);
+    st_chunk<Z, 2>(P.acc + t, t2);
+  } else if (S == 2 || S == 3) {
+    Z av[2];
+    for (int q = 0; q < 2; ++q) t2[q] = zaxpy(S == 2 ? P.dt_2 : P.dt, k[q], yv[q]);
+    st_chunk<Z, 2>((S == 2 ? P.zB : P.zA) + t, t2);
+    ld_chunk<Z, 2>(P.acc + t, av);
+    for (int q = 0; q < 2; ++q) t2[q] = zaxpy(P.dt_62, k[q], av[q]);
+    st_chunk<Z, 2>(P.acc + t, t2);
+  } else {
+    Z av[2];
+    ld_chunk<Z, 2>(P.acc + t, av);
+    for (int q = 0; q < 2; ++q) t2[q] = zaxpy(P.dt_6, k[q], av[q]);
+    st_chunk<Z, 2>(P.y + t, t2);
+    const int64_t p = P.ring ? ring_slot(P.dir, i, P.Nt, P.R, P.Nstore) : -1;
+    if (p >= 0 && RSVDT_CHECK_INDEX(p < P.Nstore, 2)) st_chunk<Z, 2>(P.ring + p * NK + t, t2);
+  }
+}
+
 size_t step_args_size(int prec) { return prec == RSVDT_PREC_C64 ? sizeof(StepArgs<z64>) : sizeof(StepArgs<z128>); }
 
 // Host copy of ctx's stage arguments for direction dir with the batch's
@@ -1534,9 +1690,19 @@ static bool launch_batched_t(cudaStream_t st, const void *args, const int2 *work
   }
 }
 
-// One batched RK4 step (four launches) on stream st.
+// One batched RK4 step (four launches) on stream st. kv = 2 (complex64,
+// fs = 1, every problem's k even): two test vectors per lane.
 bool launch_batched_step(cudaStream_t st, int prec, const void *args, const int2 *work, int nwork, int threads,
-                         int fs, int64_t *step) {
+                         int fs, int64_t *step, int kv) {
+  if (kv == 2) {
+    if (prec != RSVDT_PREC_C64 || fs != 1) return false;
+    const StepArgs<z64> *P = (const StepArgs<z64> *)args;
+    launch_pdl(k_stage_batched_pair<1>, nwork, threads, 0, st, P, work, step);
+    launch_pdl(k_stage_batched_pair<2>, nwork, threads, 0, st, P, work, step);
+    launch_pdl(k_stage_batched_pair<3>, nwork, threads, 0, st, P, work, step);
+    launch_pdl(k_stage_batched_pair<4>, nwork, threads, 0, st, P, work, step);
+    return true;
+  }
   if (prec == RSVDT_PREC_C64) return launch_batched_t<z64>(st, args, work, nwork, threads, fs, step);
   return launch_batched_t<z128>(st, args, work, nwork, threads, fs, step);
 }

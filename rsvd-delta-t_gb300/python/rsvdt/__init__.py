@@ -44,7 +44,8 @@ EXPORTED = [
     "rsvdt_set_lanes_per_row", "rsvdt_get_lanes_per_row", "rsvdt_get_timings", "rsvdt_reset_timings",
     "rsvdt_batch_create", "rsvdt_batch_destroy", "rsvdt_batch_last_error", "rsvdt_batch_add",
     "rsvdt_batch_set_sketch", "rsvdt_batch_random_sketch", "rsvdt_batch_run", "rsvdt_batch_get_results",
-    "rsvdt_batch_get_grid", "rsvdt_batch_get_tuning", "rsvdt_batch_launch_count",
+    "rsvdt_batch_get_grid", "rsvdt_batch_get_tuning", "rsvdt_batch_values_per_lane", "rsvdt_batch_set_launch_shape",
+    "rsvdt_batch_launch_count",
     "rsvdt_mlp_create", "rsvdt_mlp_destroy", "rsvdt_mlp_last_error", "rsvdt_mlp_param_count",
     "rsvdt_mlp_set_params", "rsvdt_mlp_get_params", "rsvdt_mlp_forward", "rsvdt_mlp_gradients",
     "rsvdt_mlp_train",
@@ -172,6 +173,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "rsvdt_batch_get_results": (C.c_int, [vp, C.c_int32, d, i64, d, i64, d]),
         "rsvdt_batch_get_grid": (C.c_int, [vp, C.c_int32, P(Grid)]),
         "rsvdt_batch_get_tuning": (C.c_int, [vp, P(C.c_int32), P(C.c_int32), d]),
+        "rsvdt_batch_values_per_lane": (C.c_int32, [vp]),
+        "rsvdt_batch_set_launch_shape": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32]),
         "rsvdt_batch_launch_count": (i64, [vp]),
         "rsvdt_mlp_create": (C.c_int, [C.c_int32, P(C.c_int32), C.c_uint64, P(vp)]),
         "rsvdt_mlp_destroy": (None, [vp]),
@@ -547,6 +550,13 @@ class Batch:
         th, fs, ms = C.c_int32(), C.c_int32(), C.c_double()
         self._check(self._lib.rsvdt_batch_get_tuning(self._h, C.byref(th), C.byref(fs), C.byref(ms)))
         return th.value, fs.value, ms.value
+
+    def values_per_lane(self) -> int:
+        return int(self._lib.rsvdt_batch_values_per_lane(self._h))
+
+    def set_launch_shape(self, threads: int, lanes_per_row: int = 1, values_per_lane: int = 1) -> None:
+        """Fixes the launch shape (threads = 0: autotune again)."""
+        self._check(self._lib.rsvdt_batch_set_launch_shape(self._h, threads, lanes_per_row, values_per_lane))
 
     def launch_count(self) -> int:
         return int(self._lib.rsvdt_batch_launch_count(self._h))

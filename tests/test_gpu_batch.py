@@ -115,6 +115,44 @@ def test_batch_refinement_form(built_lib):
     assert max(eref) < max(e64)
 
 
+@pytest.mark.parametrize("prec", [1, 2])
+def test_launch_shapes_give_identical_results(built_lib, prec):
+    """Every launch shape of the batched stages computes each value with the
+    same operations in the same order: the gains of a complex64 batch (and
+    of the refinement form, whose last action runs in complex128 from its
+    own work list) are bit-identical for 128/256 threads, one lane per row
+    and two test vectors per lane (all problems with an even k); the
+    autotuner's choice agrees to the complex64 rounding."""
+    import rsvdt
+    fam = [pr for pr in family() if pr["k"] % 2 == 0]
+    assert len(fam) >= 3
+    out = {}
+    for shape in ((128, 1, 1), (256, 1, 1), (128, 1, 2), (256, 1, 2), (0, 0, 0)):
+        b = rsvdt.Batch(prec)
+        for pr in fam:
+            i = b.add(params_of(rsvdt, pr), pr["A"])
+            b.set_sketch(i, pr["F"])
+        if shape[0]:
+            b.set_launch_shape(*shape)
+        b.run()
+        out[shape] = [b.get_results(i)[2] for i in range(len(fam))]
+        if shape[0]:
+            assert b.values_per_lane() == shape[2]
+        b.close()
+    base = out[(128, 1, 1)]
+    for shape, S in out.items():
+        for a, c in zip(S, base):
+            if shape[0]:
+                assert np.array_equal(a, c), shape
+            else:  # the tuner may split rows over lanes: another summation order
+                assert (np.abs(a - c) / c).max() < 1e-5
+    b = rsvdt.Batch(rsvdt.PREC_C128)
+    b.add(params_of(rsvdt, fam[0]), fam[0]["A"])
+    with pytest.raises(rsvdt.RsvdtError):
+        b.set_launch_shape(128, 1, 2)  # two values per lane need complex64 stages
+    b.close()
+
+
 def test_batch_errors(built_lib):
     import rsvdt
     b = rsvdt.Batch()
