@@ -694,6 +694,11 @@ void rsvdt_destroy(rsvdt_ctx *ctx) {
   for (void *p : ctx->allocations)
     if (p) cudaFree(p);
   if (ctx->stream && ctx->owns_stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->io_stream) {
+    cudaStreamSynchronize(ctx->io_stream);
+    cudaStreamDestroy(ctx->io_stream);
+  }
+  if (ctx->io_event) cudaEventDestroy(ctx->io_event);
   delete ctx;
 }
 
@@ -1264,12 +1269,32 @@ rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t 
     return RSVDT_ERR_CUDA;
   RSVDT_TRY(launch_colmajor_to_blk(ctx, sy, N, N, K, (z128 *)ctx->y));
   RSVDT_TRY(launch_colmajor_to_blk(ctx, sf, N, N, K, (z128 *)ctx->F3));
-  RSVDT_TRY(run_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, prec, i0, nsteps, true));
-  RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->y, N, K, sy, N));
-  RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->F3, N, K, sf, N));
-  if (!cuda_ok(ctx, cudaMemcpyAsync(y, sy, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download") ||
-      !cuda_ok(ctx, cudaMemcpyAsync(F3, sf, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download"))
-    return RSVDT_ERR_CUDA;
+  const int d = dir == RSVDT_DIRECT ? 1 : 0;
+  if (nsteps >= 1 && step_lanes(ctx) == 1) {
+    // F3 is final after the last step's stage 1: its transpose and download
+    // run on a second stream while stages 2-4 run.
+    if (!ctx->io_stream &&
+        (!cuda_ok(ctx, cudaStreamCreateWithFlags(&ctx->io_stream, cudaStreamNonBlocking), "stream create") ||
+         !cuda_ok(ctx, cudaEventCreateWithFlags(&ctx->io_event, cudaEventDisableTiming), "event create")))
+      return RSVDT_ERR_CUDA;
+    RSVDT_TRY(run_steps(ctx, d, prec, i0, nsteps - 1, true));
+    RSVDT_TRY(run_last_step_split(ctx, d, prec, i0 + nsteps - 1, ctx->io_event));
+    if (!cuda_ok(ctx, cudaStreamWaitEvent(ctx->io_stream, ctx->io_event, 0), "wait")) return RSVDT_ERR_CUDA;
+    RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->F3, N, K, sf, N, ctx->io_stream));
+    if (!cuda_ok(ctx, cudaMemcpyAsync(F3, sf, bytes, cudaMemcpyDeviceToHost, ctx->io_stream), "download"))
+      return RSVDT_ERR_CUDA;
+    RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->y, N, K, sy, N));
+    if (!cuda_ok(ctx, cudaMemcpyAsync(y, sy, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download") ||
+        !cuda_ok(ctx, cudaStreamSynchronize(ctx->io_stream), "sync"))
+      return RSVDT_ERR_CUDA;
+  } else {
+    RSVDT_TRY(run_steps(ctx, d, prec, i0, nsteps, true));
+    RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->y, N, K, sy, N));
+    RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->F3, N, K, sf, N));
+    if (!cuda_ok(ctx, cudaMemcpyAsync(y, sy, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download") ||
+        !cuda_ok(ctx, cudaMemcpyAsync(F3, sf, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download"))
+      return RSVDT_ERR_CUDA;
+  }
   return cuda_ok(ctx, cudaStreamSynchronize(ctx->stream), "sync") ? RSVDT_OK : RSVDT_ERR_CUDA;
 }
 

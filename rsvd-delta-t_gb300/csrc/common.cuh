@@ -129,6 +129,10 @@ struct rsvdt_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool owns_stream = true;  // false when the stream belongs to a batch
+  // rsvdt_rk4_steps: a second stream and an event for reading F3 back while
+  // the last step's stages 2-4 run (created on first use).
+  cudaStream_t io_stream = nullptr;
+  cudaEvent_t io_event = nullptr;
   int64_t launches = 0;
   std::string err;
 
@@ -264,6 +268,7 @@ void launch_set_step(cudaStream_t st, int64_t *step, int64_t i);
 rsvdt_status launch_unforced_steps(rsvdt_ctx *ctx, int dir, z128 *cols, int64_t ncols,
                                    int64_t nsteps);
 int step_lanes(const rsvdt_ctx *ctx);
+rsvdt_status run_last_step_split(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1);
 rsvdt_status debug_index_status(rsvdt_ctx *ctx);
 rsvdt_status launch_trans_steps(rsvdt_ctx *ctx, double dt, z128 *y, z128 *work, int64_t nsteps,
                                 cudaGraphExec_t *graph);
@@ -271,7 +276,7 @@ rsvdt_status launch_trans_steps(rsvdt_ctx *ctx, double dt, z128 *y, z128 *work, 
 rsvdt_status launch_colmajor_to_blk(rsvdt_ctx *ctx, const z128 *src, int64_t rows, int64_t ld,
                                     int64_t C, z128 *dst);
 rsvdt_status launch_blk_to_colmajor(rsvdt_ctx *ctx, const z128 *src, int64_t rows, int64_t C,
-                                    z128 *dst, int64_t ld);
+                                    z128 *dst, int64_t ld, cudaStream_t st = nullptr);
 rsvdt_status apply_weight(rsvdt_ctx *ctx, const DevCSR &M, const z128 *in, z128 *out,
                           int64_t C);
 rsvdt_status cholqr2(rsvdt_ctx *ctx, z128 *blk, int64_t rows, int64_t nw, int64_t K,

@@ -69,9 +69,9 @@ rsvdt_status launch_colmajor_to_blk(rsvdt_ctx *ctx, const z128 *src, int64_t row
 }
 
 rsvdt_status launch_blk_to_colmajor(rsvdt_ctx *ctx, const z128 *src, int64_t rows, int64_t C,
-                                    z128 *dst, int64_t ld) {
+                                    z128 *dst, int64_t ld, cudaStream_t st) {
   if ((C + 31) / 32 > 65535) return set_err(ctx, RSVDT_ERR_ARG, "too many columns (%lld)", (long long)C);
-  k_row_to_col<<<tgrid(rows, C), dim3(32, 8), 0, ctx->stream>>>(src, rows, C, dst, ld);
+  k_row_to_col<<<tgrid(rows, C), dim3(32, 8), 0, st ? st : ctx->stream>>>(src, rows, C, dst, ld);
   ctx->launches += 1;
   return cuda_ok(ctx, cudaGetLastError(), "transpose") ? RSVDT_OK : RSVDT_ERR_CUDA;
 }

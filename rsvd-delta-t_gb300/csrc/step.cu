@@ -951,6 +951,27 @@ static rsvdt_status run_steps_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t nst
   return RSVDT_OK;
 }
 
+// Step i as four stage launches with `after_stage1` recorded between stages
+// 1 and 2 (F3, the forcing at the step's end, is final from there on):
+// rsvdt_rk4_steps reads F3 back on a second stream meanwhile. Row kernels
+// (one lane per row) only.
+rsvdt_status run_last_step_split(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1) {
+  k_set_step<<<1, 1, 0, ctx->stream>>>(ctx->d_step, i);
+  if (prec == RSVDT_PREC_C64) {
+    auto P = make_args<z64>(ctx, dir, true);
+    launch_stage(1, P, ctx->stream);
+    cudaEventRecord(after_stage1, ctx->stream);
+    for (int s = 2; s <= 4; ++s) launch_stage(s, P, ctx->stream);
+  } else {
+    auto P = make_args<z128>(ctx, dir, true);
+    launch_stage(1, P, ctx->stream);
+    cudaEventRecord(after_stage1, ctx->stream);
+    for (int s = 2; s <= 4; ++s) launch_stage(s, P, ctx->stream);
+  }
+  ctx->launches += 5;
+  return cuda_ok(ctx, cudaGetLastError(), "rk4 step") ? RSVDT_OK : RSVDT_ERR_CUDA;
+}
+
 // Lanes per (row, test vector) for a context's stepping: 1 runs the stage
 // kernels above; 2, 4 or 8 runs the batched stage kernel (below) as a
 // batch of one, whose FS lanes split a row's nonzeros and forcing slabs.

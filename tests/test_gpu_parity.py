@@ -129,6 +129,30 @@ def test_rk4_steps_continue_and_restage(built_lib):
     ctx.close()
 
 
+@pytest.mark.parametrize("nsteps", [1, 9])
+def test_rk4_steps_with_row_kernels_match_oracle(built_lib, nsteps):
+    """rsvdt_rk4_steps on the one-lane-per-row kernels, whose last step reads
+    F3 back on a second stream while stages 2-4 run: y and F3 against the
+    oracle, for a single step and for several."""
+    A, cfg = small_gl()
+    k = 3
+    ctx = make_ctx(A, cfg, k=k)
+    ctx.set_lanes_per_row(1)
+    g = ctx.grid()
+    N, nwe = A.shape[0], g.Nw_eff
+    F = synth.complex_normal(N, k * nwe, 25)
+    y0 = synth.complex_normal(N, k, 26)
+    F30 = synth.complex_normal(N, k, 27)
+    ctx.set_sketch(F)
+    y, F3 = ctx.rk4_steps(0, 11, nsteps, y0.copy(), F30.copy())
+    orc = make_oracle(A, cfg)
+    for ik in range(k):
+        Fk = F[:, [iw * k + ik for iw in range(nwe)]]
+        yo, F3o = orc.rk4_steps(0, Fk, 11, nsteps, y0[:, ik], F30[:, ik])
+        assert rel(y[:, ik], yo) < 1e-11 and rel(F3[:, ik], F3o) < 1e-11
+    ctx.close()
+
+
 @pytest.mark.parametrize("direction,tr", [(1, False), (0, False), (1, True), (0, True)])
 def test_action_matches_oracle(built_lib, direction, tr):
     """One resolvent action (TSActionRK4 + DFT or transient removal)."""
