@@ -5,15 +5,16 @@
 // the DFT, the Gram products of all frequencies and the weight products
 // each read a row once, coalesced.
 //
-//  - QRAllFreqs (SourceCode/QRAllFreqs.c:22-32) becomes batched CholQR2 over
-//    all frequencies: FP64 Gram G_iw = Y_iw^H Y_iw by row chunks, a
+//  - QRAllFreqs (SourceCode/QRAllFreqs.c:22-32) becomes batched CholQR over
+//    all frequencies (one shifted pass, then plain passes): FP64 Gram
+//    G_iw = Y_iw^H Y_iw by row chunks (the k(k+1)/2 upper pairs only), a
 //    deterministic chunk reduction, a per-frequency Cholesky G = R^H R, then
-//    Y_iw <- Y_iw R^{-1}; twice. R keeps a real positive diagonal, which is
-//    the normalisation of SLEPc's Gram-Schmidt, so Q matches column for
-//    column.
-//  - SVDAllFreqs (SourceCode/SVDAllFreqs.c:34-56) becomes CholQR2 (Y = QR)
-//    followed by a one-sided Jacobi SVD of each k x k R (R = U_R S W^H) and
-//    U = Q U_R.
+//    Y_iw <- Y_iw R^{-1}. R keeps a real positive diagonal, which is the
+//    normalisation of SLEPc's Gram-Schmidt, so Q matches column for column.
+//  - SVDAllFreqs (SourceCode/SVDAllFreqs.c:34-56) becomes the same CholQR
+//    (Y = QR) followed by a one-sided Jacobi SVD of each k x k R
+//    (R = U_R S W^H) and U = Q U_R.
+//  All of it is FP64-bound on GB300 (k x k work per row and frequency).
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>

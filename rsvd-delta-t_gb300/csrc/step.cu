@@ -29,13 +29,17 @@
 // positive one (the reference evaluates it from a much larger argument,
 // which carries its own rounding).
 //
-// Three kernel families: k_stage (one thread per row and test vector, any
+// Stage kernel families: k_stage (one thread per row and test vector, any
 // CSR or block-CSR operator, any k); for 5x5 block-CSR with k a
 // compile-time constant, k_bstage (complex64: one lane per block row and
 // group of test vectors, which reads every gathered k-vector row as one
 // contiguous 16-byte-per-lane access, for HBM-bound stages) and k_rstage
 // (complex128: one thread per row with all k test vectors in registers,
-// full warps for the FP64-bound stages).
+// full warps for the FP64-bound stages); for small problems and batches,
+// k_stage_batched (lanes split a row's nonzeros and slabs) and
+// k_stage_batched_pair (two complex64 test vectors per lane). Stage
+// kernels are launched with programmatic dependent launch. The end of the
+// file holds the DFT of the sampled period (radix-2 FFT for Nw = 8..64).
 #include <cstdarg>
 #include <cstring>
 
