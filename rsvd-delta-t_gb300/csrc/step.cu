@@ -38,8 +38,8 @@
 // full warps for the FP64-bound stages); for small problems and batches,
 // k_stage_batched (lanes split a row's nonzeros and slabs) and
 // k_stage_batched_pair (two complex64 test vectors per lane). Stage
-// kernels are launched with programmatic dependent launch. The end of the
-// file holds the DFT of the sampled period (radix-2 FFT for Nw = 8..64).
+// kernels are launched with programmatic dependent launch. This file also
+// holds the DFT of the sampled period (radix-2 FFT for Nw = 8..64).
 #include <cstdarg>
 #include <cstring>
 
