@@ -343,9 +343,20 @@ __global__ void __launch_bounds__(256) k_apply_upper(z128 *__restrict__ Y, int64
   const z128 *x = sm + local * K;
   z128 s1 = zmake<z128>(0, 0), s2 = zmake<z128>(0, 0);
   const int b1 = j, b2 = K - 1 - j;
-  for (int a = 0; a <= b1; ++a) zmac(s1, x[a], m[a * K + b1]);
-  if (b2 != b1)
-    for (int a = 0; a <= b2; ++a) zmac(s2, x[a], m[a * K + b2]);
+  // One loop of K + 1 products for every lane (b1 + 1 for output b1, then
+  // b2 + 1 for output b2), so the warp's lanes do not diverge at the switch;
+  // each output's products are summed in ascending a.
+  const int n1 = b1 + 1, ntot = b2 != b1 ? K + 1 : n1;
+  for (int q = 0; q < ntot; ++q) {
+    const bool first = q < n1;
+    const int a = first ? q : q - n1, b = first ? b1 : b2;
+    z128 acc = first ? s1 : s2;
+    zmac(acc, x[a], m[a * K + b]);
+    if (first)
+      s1 = acc;
+    else
+      s2 = acc;
+  }
   z128 *y = Y + n * stride + (int64_t)iw * K;
   y[b1] = s1;
   if (b2 != b1) y[b2] = s2;
