@@ -106,3 +106,17 @@ def test_c_and_ctypes_struct_layouts_agree(built_lib, tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for fname, _ in py._fields_:
             assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def test_debug_build_compiles_and_identifies_itself(built_lib):
+    """The bounds-checked build (-DRSVDT_DEBUG) compiles, exports the same
+    symbols and reports itself; the release build reports 0."""
+    import ctypes
+
+    from rsvdt import build
+
+    dbg = ctypes.CDLL(build.build_library(debug=True))
+    rel = ctypes.CDLL(built_lib)
+    assert dbg.rsvdt_debug_build() == 1 and rel.rsvdt_debug_build() == 0
+    missing = [n for n in declared_functions() if not hasattr(dbg, n)]
+    assert not missing, missing
