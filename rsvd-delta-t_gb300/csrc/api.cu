@@ -1360,6 +1360,21 @@ rsvdt_status rsvdt_set_lanes_per_row(rsvdt_ctx *ctx, int32_t lanes) {
 
 int32_t rsvdt_get_lanes_per_row(const rsvdt_ctx *ctx) { return ctx ? step_lanes(ctx) : 0; }
 
+rsvdt_status rsvdt_set_step_engine(rsvdt_ctx *ctx, int32_t engine) {
+  if (!ctx) return RSVDT_ERR_ARG;
+  if (engine != RSVDT_ENGINE_AUTO && engine != RSVDT_ENGINE_STAGES && engine != RSVDT_ENGINE_CLUSTER)
+    return set_err(ctx, RSVDT_ERR_ARG, "step engine must be 0 (automatic), 1 (stages) or 2 (cluster), not %d",
+                   (int)engine);
+  ctx->engine = engine;
+  return RSVDT_OK;
+}
+
+int32_t rsvdt_get_step_engine(const rsvdt_ctx *ctx) {
+  if (!ctx) return 0;
+  int C = 0, threads = 0;
+  return use_cluster_engine(ctx, ctx->act_prec, &C, &threads) ? RSVDT_ENGINE_CLUSTER : RSVDT_ENGINE_STAGES;
+}
+
 rsvdt_status rsvdt_device_memory(int64_t *free_bytes, int64_t *total_bytes) {
   size_t fr = 0, tot = 0;
   if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {

@@ -203,6 +203,10 @@ struct rsvdt_ctx {
   // step_lanes): lanes per row (0 = chosen from the size), the argument
   // blocks of both directions, the work list and the cached graphs.
   int lanes_override = 0;
+  // rsvdt_step_engine, and the cluster engine's forcing buffer.
+  int engine = RSVDT_ENGINE_AUTO;
+  void *cl_fbuf = nullptr;
+  size_t cl_bytes = 0;
   // rsvdt_set_checkpoint: called after the second QR of every power sweep.
   rsvdt_checkpoint_fn ckpt_fn = nullptr;
   void *ckpt_user = nullptr;
@@ -268,6 +272,7 @@ void launch_set_step(cudaStream_t st, int64_t *step, int64_t i);
 rsvdt_status launch_unforced_steps(rsvdt_ctx *ctx, int dir, z128 *cols, int64_t ncols,
                                    int64_t nsteps);
 int step_lanes(const rsvdt_ctx *ctx);
+bool use_cluster_engine(const rsvdt_ctx *ctx, int prec, int *C, int *threads);
 rsvdt_status run_last_step_split(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1);
 rsvdt_status debug_index_status(rsvdt_ctx *ctx);
 rsvdt_status launch_trans_steps(rsvdt_ctx *ctx, double dt, z128 *y, z128 *work, int64_t nsteps,

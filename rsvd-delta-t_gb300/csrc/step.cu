@@ -1056,7 +1056,232 @@ static rsvdt_status run_steps_small(rsvdt_ctx *ctx, int dir, int prec, int64_t i
   return RSVDT_OK;
 }
 
+// ------------------------------------------- the cluster engine (small problems)
+//
+// A small problem's step is four short dependent stages; launched one by
+// one, each costs a launch (~5 us on GB300) for ~1 us of work. The cluster
+// engine splits the step differently: the forcing synthesis, which does not
+// depend on the state and is the FP64 bulk of a step, runs for G steps at
+// once over the whole GPU (k_forcing_steps); then one thread-block cluster
+// (up to 16 CTAs, one per SM of a GPC) runs the G steps' four stages back
+// to back, one thread per (row, test vector), with a hardware cluster
+// barrier between stages (k_cluster_steps). Each value is computed with the
+// same operations in the same order as the one-lane stage kernels
+// (k_stage): bit-identical results.
+
+static const int kClusterSteps = 64;  // G: steps per forcing / cluster launch pair
+static const int kClusterThreads = 512;         // most threads per CTA (one per value)
+static const int64_t kClusterAutoMax = 8192;   // largest rows x test vectors AUTO hands to the engine
+
+// A load through L2 only (a value another SM wrote in the same launch).
+template <class Z>
+__device__ __forceinline__ Z ld_l2(const Z *p) {
+  if constexpr (sizeof(Z) == 16) {
+    const double2 t = __ldcg(reinterpret_cast<const double2 *>(p));
+    return zmake<Z>(t.x, t.y);
+  } else {
+    const float2 t = __ldcg(reinterpret_cast<const float2 *>(p));
+    return zmake<Z>(t.x, t.y);
+  }
+}
+
+template <class Z>
+__global__ void __launch_bounds__(256) k_forcing_steps(const StepArgs<Z> P, int64_t i0, int G, Z *__restrict__ fbuf) {
+  const int64_t NK = P.N * P.K;
+  const int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (u >= NK * G) return;
+  const int g = (int)(u / NK);
+  const int64_t t = u - (int64_t)g * NK;
+  const int64_t n = t / P.K;
+  const int kc = (int)(t - n * P.K);
+  Z f2 = zmake<Z>(0, 0), f3 = zmake<Z>(0, 0);
+  if (P.Fh) {
+    int64_t j2, j3;
+    step_idx(P.dir, i0 + g, P.two_ns, j2, j3);
+    forcing2(P, n, kc, P.tab + j2 * P.Nw, P.tab + j3 * P.Nw, 0, 1, f2, f3);
+  }
+  fbuf[(2 * (int64_t)g) * NK + t] = f2;
+  fbuf[(2 * (int64_t)g + 1) * NK + t] = f3;
+}
+
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// acc += sum_j A[n,j] x[j][kc] over the row (k_stage's row_product), the
+// gathered values read through L2: other CTAs of the cluster wrote them
+// in this launch.
+template <class Z>
+__device__ __forceinline__ void row_product_l2(const StepArgs<Z> &P, int64_t n, int kc, const Z *x, Z &acc) {
+  const int K = P.K;
+  if (P.bs == 0) {
+    const int32_t b = __ldg(P.rowptr + n), e = __ldg(P.rowptr + n + 1);
+    for (int32_t j = b; j < e; ++j) {
+      const int32_t cj = __ldg(P.col + j);
+      if (!RSVDT_CHECK_INDEX(cj >= 0 && cj < P.N, 0)) continue;
+      zmac(acc, P.val[j], ld_l2<Z>(x + (int64_t)cj * K + kc));
+    }
+  } else {
+    const int bs = P.bs;
+    const int64_t br = n / bs;
+    const int r = (int)(n - br * bs);
+    const int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
+    for (int32_t j = b; j < e; ++j) {
+      const int32_t cb = __ldg(P.col + j);
+      if (!RSVDT_CHECK_INDEX(cb >= 0 && cb < P.N / bs, 1)) continue;
+      const int64_t c0 = (int64_t)cb * bs;
+      const Z *blkrow = P.val + (int64_t)j * P.bstride + r * bs;
+      for (int c = 0; c < bs; ++c) zmac(acc, blkrow[c], ld_l2<Z>(x + (c0 + c) * K + kc));
+    }
+  }
+}
+
+// Steps i0 .. i0+G-1 of the whole problem on one cluster; fbuf holds each
+// step's F2 and F3 (k_forcing_steps). Every thread of every CTA passes every
+// barrier (no thread leaves early).
+template <class Z>
+__global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_steps(const StepArgs<Z> P, int64_t i0, int G,
+                                                        const Z *__restrict__ fbuf) {
+  const int64_t NK = P.N * P.K;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool valid = t < NK;
+  const int64_t n = valid ? t / P.K : 0;
+  const int kc = valid ? (int)(t - n * P.K) : 0;
+  Z y = zmake<Z>(0, 0), f3old = zmake<Z>(0, 0), acc = zmake<Z>(0, 0);
+  if (valid) {
+    y = P.y[t];
+    f3old = P.F3[t];
+  }
+  for (int g = 0; g < G; ++g) {
+    const int64_t i = i0 + g;
+    Z f2 = zmake<Z>(0, 0), f3 = zmake<Z>(0, 0);
+    if (valid) {
+      f2 = fbuf[(2 * (int64_t)g) * NK + t];
+      f3 = fbuf[(2 * (int64_t)g + 1) * NK + t];
+      Z k = f3old;  // stage 1: k1 = A y + F3 of the previous step
+      row_product_l2(P, n, kc, P.y, k);
+      P.zA[t] = zaxpy(P.dt_2, k, y);
+      acc = zaxpy(P.dt_6, k, y);
+      f3old = f3;
+    }
+    cluster_barrier();
+    if (valid) {
+      Z k = f2;  // stage 2
+      row_product_l2(P, n, kc, P.zA, k);
+      P.zB[t] = zaxpy(P.dt_2, k, y);
+      acc = zaxpy(P.dt_62, k, acc);
+    }
+    cluster_barrier();
+    if (valid) {
+      Z k = f2;  // stage 3
+      row_product_l2(P, n, kc, P.zB, k);
+      P.zA[t] = zaxpy(P.dt, k, y);
+      acc = zaxpy(P.dt_62, k, acc);
+    }
+    cluster_barrier();
+    if (valid) {
+      Z k = f3;  // stage 4
+      row_product_l2(P, n, kc, P.zA, k);
+      y = zaxpy(P.dt_6, k, acc);
+      P.y[t] = y;
+      const int64_t p = P.ring ? ring_slot(P.dir, i, P.Nt, P.R, P.Nstore) : -1;
+      if (p >= 0 && RSVDT_CHECK_INDEX(p < P.Nstore, 2)) P.ring[p * NK + t] = y;
+    }
+    cluster_barrier();
+  }
+  if (valid) {
+    P.F2[t] = fbuf[(2 * (int64_t)(G - 1)) * NK + t];
+    P.F3[t] = f3old;
+    P.acc[t] = acc;
+  }
+  if (t == 0) {
+    P.step[0] = i0 + G;
+    P.step[1] = i0 + G - 1;
+  }
+}
+
+// Cluster size and threads per CTA for a problem of NK values (0: the
+// engine does not apply).
+template <class Z>
+static int cluster_shape(int64_t NK, int *threads) {
+  static int max_cluster = -1;
+  if (max_cluster < 0) {
+    max_cluster = 0;
+    if (cudaFuncSetAttribute(k_cluster_steps<Z>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(16);
+      cfg.blockDim = dim3(kClusterThreads);
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = 16;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int c = 0;
+      if (cudaOccupancyMaxPotentialClusterSize(&c, k_cluster_steps<Z>, &cfg) == cudaSuccess) max_cluster = c;
+    }
+    cudaGetLastError();
+    if (max_cluster > 16) max_cluster = 16;
+  }
+  // As many SMs as a cluster can have (the stages' FP64 work spreads over
+  // them), one thread per value.
+  if (max_cluster < 1) return 0;
+  const int64_t per = (NK + max_cluster - 1) / max_cluster;
+  if (per > kClusterThreads) return 0;
+  *threads = (int)((per + 31) / 32 * 32);
+  return max_cluster;
+}
+
+template <class Z>
+static rsvdt_status run_steps_cluster_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t nsteps, int C, int threads) {
+  auto P = make_args<Z>(ctx, dir, true);
+  const int64_t NK = P.N * P.K;
+  const size_t need = sizeof(Z) * 2 * (size_t)NK * kClusterSteps;
+  if (ctx->cl_bytes < need) {
+    dfree(ctx, ctx->cl_fbuf);
+    ctx->cl_fbuf = dalloc(ctx, need);
+    ctx->cl_bytes = ctx->cl_fbuf ? need : 0;
+    if (!ctx->cl_fbuf) return set_err(ctx, RSVDT_ERR_OOM, "forcing buffer allocation failed");
+  }
+  Z *fbuf = (Z *)ctx->cl_fbuf;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)C);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  for (int64_t done = 0; done < nsteps;) {
+    const int G = (int)std::min<int64_t>(kClusterSteps, nsteps - done);
+    const int64_t i = i0 + done;
+    k_forcing_steps<Z><<<grid_for(NK * G, 256), 256, 0, ctx->stream>>>(P, i, G, fbuf);
+    if (!cuda_ok(ctx, cudaLaunchKernelEx(&cfg, k_cluster_steps<Z>, P, i, G, (const Z *)fbuf), "cluster steps"))
+      return RSVDT_ERR_CUDA;
+    ctx->launches += 2;
+    done += G;
+  }
+  return cuda_ok(ctx, cudaGetLastError(), "cluster steps") ? RSVDT_OK : RSVDT_ERR_CUDA;
+}
+
+// Whether the cluster engine runs this context's steps (and its shape).
+bool use_cluster_engine(const rsvdt_ctx *ctx, int prec, int *C, int *threads) {
+  if (ctx->engine == RSVDT_ENGINE_STAGES) return false;
+  const int64_t NK = ctx->N * ctx->Ks;
+  if (ctx->engine == RSVDT_ENGINE_AUTO && NK > kClusterAutoMax) return false;
+  *C = prec == RSVDT_PREC_C64 ? cluster_shape<z64>(NK, threads) : cluster_shape<z128>(NK, threads);
+  return *C > 0;
+}
+
 rsvdt_status run_steps(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_t nsteps, bool) {
+  int C = 0, threads = 0;
+  if (nsteps > 0 && use_cluster_engine(ctx, prec, &C, &threads))
+    return prec == RSVDT_PREC_C64 ? run_steps_cluster_t<z64>(ctx, dir, i0, nsteps, C, threads)
+                                  : run_steps_cluster_t<z128>(ctx, dir, i0, nsteps, C, threads);
   const int fs = step_lanes(ctx);
   if (fs > 1) return run_steps_small(ctx, dir, prec, i0, nsteps, fs);
   if (prec == RSVDT_PREC_C64) return run_steps_t<z64>(ctx, dir, i0, nsteps);

@@ -25,6 +25,7 @@ LIB_PATH = _build.LIB_PATH
 OK, ERR_ARG, ERR_IO, ERR_OOM, ERR_CUDA, ERR_NOT_SPD, ERR_DIVERGED, ERR_TIMEOUT, ERR_STATE = range(9)
 ADJOINT, DIRECT = 0, 1
 PREC_C128, PREC_C64, PREC_C64_REFINE = 0, 1, 2
+ENGINE_AUTO, ENGINE_STAGES, ENGINE_CLUSTER = 0, 1, 2
 W_F_SQRT_INV, B, C_OUT, W_Q_SQRT, W_Q_SQRT_INV = range(5)
 
 STATUS_NAMES = {0: "OK", 1: "ARG", 2: "IO", 3: "OOM", 4: "CUDA", 5: "NOT_SPD", 6: "DIVERGED",
@@ -42,6 +43,7 @@ EXPORTED = [
     "rsvdt_qr_all_freqs_noalloc", "rsvdt_trans_grid", "rsvdt_trans_run",
     "rsvdt_set_capacity_mode", "rsvdt_get_capacity", "rsvdt_get_result_cols", "rsvdt_device_memory",
     "rsvdt_set_lanes_per_row", "rsvdt_get_lanes_per_row", "rsvdt_get_timings", "rsvdt_reset_timings",
+    "rsvdt_set_step_engine", "rsvdt_get_step_engine",
     "rsvdt_batch_create", "rsvdt_batch_destroy", "rsvdt_batch_last_error", "rsvdt_batch_add",
     "rsvdt_batch_set_sketch", "rsvdt_batch_random_sketch", "rsvdt_batch_run", "rsvdt_batch_get_results",
     "rsvdt_batch_get_grid", "rsvdt_batch_get_tuning", "rsvdt_batch_values_per_lane", "rsvdt_batch_set_launch_shape",
@@ -159,6 +161,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "rsvdt_reset_timings": (C.c_int, [vp]),
         "rsvdt_set_lanes_per_row": (C.c_int, [vp, C.c_int32]),
         "rsvdt_get_lanes_per_row": (C.c_int32, [vp]),
+        "rsvdt_set_step_engine": (C.c_int, [vp, C.c_int32]),
+        "rsvdt_get_step_engine": (C.c_int32, [vp]),
         "rsvdt_get_result_cols": (C.c_int, [vp, P(i64), i64, d, i64, d, i64]),
         "rsvdt_trans_grid": (C.c_int, [vp, P(TransParams), P(TransInfo)]),
         "rsvdt_trans_run": (C.c_int, [vp, P(TransParams), d, d, TRANS_SNAPSHOT_FN, TRANS_ESTIMATE_FN, vp,
@@ -406,6 +410,14 @@ class Context:
 
     def lanes_per_row(self) -> int:
         return int(self._lib.rsvdt_get_lanes_per_row(self._h))
+
+    def set_step_engine(self, engine: int) -> None:
+        """ENGINE_AUTO, ENGINE_STAGES or ENGINE_CLUSTER (rsvdt_set_step_engine)."""
+        self._check(self._lib.rsvdt_set_step_engine(self._h, engine))
+
+    def step_engine(self) -> int:
+        """The engine the next stepping uses (STAGES or CLUSTER)."""
+        return int(self._lib.rsvdt_get_step_engine(self._h))
 
     # -------------------------------------------------------- capacity mode
     def set_capacity_mode(self, kc: int = 0, u_c64: bool = False) -> None:

@@ -333,6 +333,45 @@ def test_bcsr_matches_csr_and_oracle(built_lib, lanes):
     ctx_c.close()
 
 
+@pytest.mark.parametrize("op,prec", [("csr", 0), ("csr", 1), ("bcsr", 0), ("bcsr", 1)])
+def test_cluster_engine_is_bit_identical(built_lib, op, prec):
+    """The cluster engine (forcing of 64 steps over the GPU, then the steps'
+    stages on one thread-block cluster) against the one-lane stage kernels:
+    identical bits after whole actions in both directions, with and without
+    transient removal, and through rsvdt_rk4_steps from an arbitrary step.
+    CSR: the 64-node Ginzburg-Landau operator, k = 3; block CSR: the 4^3
+    five-field operator, k = 2."""
+    import rsvdt
+    if op == "csr":
+        A, cfg = small_gl()
+        bcsr, k = None, 3
+    else:
+        bcsr = synth.op3d_blocks(n=4, shift=0.5, seed=3)
+        A = synth.bcsr_to_csr(*bcsr)
+        cfg, k = dict(w=0.5, Nw=8, dt=0.05, TransientLength=2 * np.pi / 0.5), 2
+    out = {}
+    for engine in (rsvdt.ENGINE_STAGES, rsvdt.ENGINE_CLUSTER):
+        res = []
+        for tr in (False, True):
+            ctx = make_ctx(A, cfg, k=k, tr=tr, prec=prec, bcsr=bcsr)
+            ctx.set_lanes_per_row(1)
+            ctx.set_step_engine(engine)
+            assert ctx.step_engine() == engine
+            F = synth.complex_normal(A.shape[0], k * ctx.grid().Nw_eff, 6)
+            for d in (1, 0):
+                ctx.set_sketch(F)
+                ctx.action(d)
+                res.append(ctx.get_block())
+            if prec == 0 and not tr:
+                y0 = synth.complex_normal(A.shape[0], k, 7)
+                f0 = synth.complex_normal(A.shape[0], k, 8)
+                res.extend(ctx.rk4_steps(1, 37, 70, y0, f0))
+            ctx.close()
+        out[engine] = res
+    for a, b in zip(out[rsvdt.ENGINE_STAGES], out[rsvdt.ENGINE_CLUSTER]):
+        assert np.isfinite(a).all() and np.array_equal(a, b)
+
+
 def test_c64_form_close_to_c128(built_lib):
     """Precision form: complex64 operator/state/stages with FP32 accumulation,
     FP64 DFT/QR/SVD. Gains within 1e-3 of the complex128 plain form."""
