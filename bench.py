@@ -288,10 +288,10 @@ def gl1_form(threads: int):
     A = wl.csr.toarray()
     om = np.array([(i if i <= 31 else i - 64) * 0.1 for i in range(64)])
     sd = np.array([np.linalg.svd(np.linalg.inv(1j * w * np.eye(500) - A), compute_uv=False)[:3] for w in om]).T
-    for q, lanes in ((0, 0), (1, 0), (0, 1)):
+    for q, engine in ((0, rsvdt.ENGINE_AUTO), (1, rsvdt.ENGINE_AUTO), (0, rsvdt.ENGINE_STAGES)):
         ctx = rsvdt.Context(rsvdt.default_params(k=10, q=q, Nw=64, w=0.1, dt=wl.dt_in,
                                                  TransientLength=wl.transient_length, Display=0))
-        ctx.set_lanes_per_row(lanes)
+        ctx.set_step_engine(engine)
         ctx.set_operator(wl.csr)
         ctx.set_sketch(F)
         ctx.run()
@@ -301,13 +301,13 @@ def gl1_form(threads: int):
         ctx.run()
         S = ctx.get_results(U=False, V=False)[2]
         t = time.perf_counter() - t0
-        used = ctx.lanes_per_row()
+        used = "cluster" if ctx.step_engine() == rsvdt.ENGINE_CLUSTER else "stages"
         ctx.close()
-        if lanes == 1:
-            out["gpu_q0_one_lane_per_row_s"] = round(t, 4)
+        if engine == rsvdt.ENGINE_STAGES:
+            out["gpu_q0_stage_launches_s"] = round(t, 4)
             continue
         out[f"gpu_q{q}_s"] = round(t, 4)
-        out["lanes_per_row"] = used
+        out["step_engine"] = used
         out[f"q{q}_gain1_vs_dense_max"] = float((np.abs(S[0] - sd[0]) / sd[0]).max())
     import oracle
 
