@@ -171,7 +171,7 @@ rsvdt_status rsvdt_power_iteration(rsvdt_ctx *ctx);
  * matrix. fn(user, sweep, ctx) is called after the second QR of every sweep
  * (sweep = 1..q), when the working block holds the forcing of that sweep's
  * direct action; fn may read it with rsvdt_get_block. Setting that block as
- * the sketch (rsvdt_set_sketch, or InputForcingDir in the driver) and
+ * the sketch (rsvdt_set_sketch, or InputForcingDir in the drop-in driver) and
  * running with q - sweep power iterations continues the sequence exactly
  * (identical results). A non-zero return stops rsvdt_power_iteration and
  * rsvdt_run with RSVDT_ERR_STATE. fn = NULL removes the hook. */

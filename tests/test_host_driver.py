@@ -70,7 +70,7 @@ def test_flag_requires_directory_and_bad_values(driver, tmp_path):
     assert r.returncode != 0 and "Must specify 'TransICDir'" in r.stderr
     r = run(driver, tmp_path, TransSaveMod="2.5")
     assert r.returncode != 0 and "no integer value" in r.stderr
-    # The driver's own key (resume points) follows the same logical syntax.
+    # The drop-in driver's own key (resume points) follows the same logical syntax.
     r = run(driver, tmp_path, SaveResumeQ="maybe")
     assert r.returncode != 0 and "Unknown logical value" in r.stderr
 

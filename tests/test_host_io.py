@@ -1,4 +1,4 @@
-"""The driver's C PETSc-binary layer (host/petsc_bin.c) against the Python
+"""The drop-in driver's C PETSc-binary layer (host/petsc_bin.c) against the Python
 reader/writer: both index widths, the tutorial operator with its trailing
 objects, the dense-as-AIJ output of MatView, vectors, and a throughput
 figure for a matrix of 5M nonzeros (printed; the parallel byte swap and
