@@ -665,10 +665,11 @@ def main():
             "roofline": {"bound": "hbm", "kernel": "k_rstage<z128,10,1> (block-row SpMM + forcing synthesis)",
                          "achieved": round(ach, 2), "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4),
                          "peak_kind": peak_kind,
-                         # DRAM bytes of one launch: the ncu capture of the same kernel on the
-                         # 32^3 operator (994.8 MB read + 97.6 MB written) scaled by N.
-                         "traffic": round(1.0924e9 * wl.N / 163840),
-                         "traffic_source": "ncu dram__bytes_read+write of k_rstage<z128,10,1> at 3D32, scaled by N",
+                         # DRAM bytes of one launch: a one-pass ncu capture of this kernel on
+                         # the 64^3 operator (7.990 GB read + 0.832 GB written), scaled by N
+                         # for other grids.
+                         "traffic": round(8.8219e9 * wl.N / 1310720),
+                         "traffic_source": "ncu dram__bytes_read+write of k_rstage<z128,10,1> at 3D64, one launch",
                          "bytes_per_launch": b["stage1"], "ms_per_launch": round(st_ms[0], 4),
                          "fp64": {"achieved_tflops": round(ach_fp64, 4), "peak_tflops": round(fp64_peak, 4),
                                   "frac": round(ach_fp64 / fp64_peak, 4),
