@@ -11,10 +11,16 @@ traffic over its device time:
 Inputs (14 GB working set) are far larger than L2, so no flush is needed.
 
 Extra keys: roofline of the dominant kernel (stage 1, timed live with CUDA
-events on the library's stream), the FP64 rate it achieves against a
-measured FP64 peak (the plain form is FP64-bound on this part), the
-complex64 precision form's step, e2e through the C ABI with host buffers,
-and the CPU baseline (the C restatement timed on the host cores).
+events on the library's stream; DRAM traffic from a one-pass ncu capture),
+the FP64 rate it achieves against a measured FP64 peak (the plain form is
+FP64-bound on this part), the complex64 precision form's step, e2e through
+the C ABI with host buffers, the CPU baseline (the C restatement timed on
+the host cores), and the side experiments: time to gains of the whole q = 1
+solve in the plain, complex64 and refinement forms with phase times; the
+48-problem batching form with the autotuned launch shapes; the 500-node
+Ginzburg-Landau configuration with its step engine and CPU baseline; with
+flags, the learned sketch (GL and 3D families) and the 128^3 capacity
+case.
 
 --impl reference times the reference's CPU algorithm (the C restatement
 in oracle/, since the reference itself needs PETSc/SLEPc/MPI) on all host
