@@ -699,6 +699,7 @@ void rsvdt_destroy(rsvdt_ctx *ctx) {
     cudaStreamDestroy(ctx->io_stream);
   }
   if (ctx->io_event) cudaEventDestroy(ctx->io_event);
+  if (ctx->up_event) cudaEventDestroy(ctx->up_event);
   delete ctx;
 }
 
@@ -1263,22 +1264,31 @@ rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t 
   }
   z128 *sy = ctx->io_stage, *sf = ctx->io_stage + N * K;
   const size_t bytes = sizeof(z128) * (size_t)N * K;
-  // Host (N x K column-major) -> device [n][k], both arrays in flight.
-  if (!cuda_ok(ctx, cudaMemcpyAsync(sy, y, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload") ||
-      !cuda_ok(ctx, cudaMemcpyAsync(sf, F3, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload"))
-    return RSVDT_ERR_CUDA;
-  RSVDT_TRY(launch_colmajor_to_blk(ctx, sy, N, N, K, (z128 *)ctx->y));
-  RSVDT_TRY(launch_colmajor_to_blk(ctx, sf, N, N, K, (z128 *)ctx->F3));
   const int d = dir == RSVDT_DIRECT ? 1 : 0;
-  if (nsteps >= 1 && step_lanes(ctx) == 1) {
-    // F3 is final after the last step's stage 1: its transpose and download
-    // run on a second stream while stages 2-4 run.
+  int C = 0, cth = 0;
+  if (nsteps >= 1 && step_lanes(ctx) == 1 && !use_cluster_engine(ctx, prec, &C, &cth)) {
     if (!ctx->io_stream &&
         (!cuda_ok(ctx, cudaStreamCreateWithFlags(&ctx->io_stream, cudaStreamNonBlocking), "stream create") ||
-         !cuda_ok(ctx, cudaEventCreateWithFlags(&ctx->io_event, cudaEventDisableTiming), "event create")))
+         !cuda_ok(ctx, cudaEventCreateWithFlags(&ctx->io_event, cudaEventDisableTiming), "event create") ||
+         !cuda_ok(ctx, cudaEventCreateWithFlags(&ctx->up_event, cudaEventDisableTiming), "event create")))
       return RSVDT_ERR_CUDA;
-    RSVDT_TRY(run_steps(ctx, d, prec, i0, nsteps - 1, true));
-    RSVDT_TRY(run_last_step_split(ctx, d, prec, i0 + nsteps - 1, ctx->io_event));
+    // The first step's forcing needs no state: it is synthesised on the
+    // context's stream while y and F3 upload on the second stream.
+    RSVDT_TRY(launch_forcing_ahead(ctx, d, prec, i0));
+    if (!cuda_ok(ctx, cudaMemcpyAsync(sy, y, bytes, cudaMemcpyHostToDevice, ctx->io_stream), "upload") ||
+        !cuda_ok(ctx, cudaMemcpyAsync(sf, F3, bytes, cudaMemcpyHostToDevice, ctx->io_stream), "upload") ||
+        !cuda_ok(ctx, cudaEventRecord(ctx->up_event, ctx->io_stream), "event") ||
+        !cuda_ok(ctx, cudaStreamWaitEvent(ctx->stream, ctx->up_event, 0), "wait"))
+      return RSVDT_ERR_CUDA;
+    RSVDT_TRY(launch_colmajor_to_blk(ctx, sy, N, N, K, (z128 *)ctx->y));
+    RSVDT_TRY(launch_colmajor_to_blk(ctx, sf, N, N, K, (z128 *)ctx->F3));
+    // F3 is final after the last step's stage 1: its transpose and download
+    // run on the second stream while stages 2-4 run.
+    RSVDT_TRY(launch_first_step_rest(ctx, d, prec, i0, nsteps == 1 ? ctx->io_event : nullptr));
+    if (nsteps >= 2) {
+      RSVDT_TRY(run_steps(ctx, d, prec, i0 + 1, nsteps - 2, true));
+      RSVDT_TRY(run_last_step_split(ctx, d, prec, i0 + nsteps - 1, ctx->io_event));
+    }
     if (!cuda_ok(ctx, cudaStreamWaitEvent(ctx->io_stream, ctx->io_event, 0), "wait")) return RSVDT_ERR_CUDA;
     RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->F3, N, K, sf, N, ctx->io_stream));
     if (!cuda_ok(ctx, cudaMemcpyAsync(F3, sf, bytes, cudaMemcpyDeviceToHost, ctx->io_stream), "download"))
@@ -1288,6 +1298,12 @@ rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t 
         !cuda_ok(ctx, cudaStreamSynchronize(ctx->io_stream), "sync"))
       return RSVDT_ERR_CUDA;
   } else {
+    // Host (N x K column-major) -> device [n][k], both arrays in flight.
+    if (!cuda_ok(ctx, cudaMemcpyAsync(sy, y, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload") ||
+        !cuda_ok(ctx, cudaMemcpyAsync(sf, F3, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload"))
+      return RSVDT_ERR_CUDA;
+    RSVDT_TRY(launch_colmajor_to_blk(ctx, sy, N, N, K, (z128 *)ctx->y));
+    RSVDT_TRY(launch_colmajor_to_blk(ctx, sf, N, N, K, (z128 *)ctx->F3));
     RSVDT_TRY(run_steps(ctx, d, prec, i0, nsteps, true));
     RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->y, N, K, sy, N));
     RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->F3, N, K, sf, N));

@@ -132,7 +132,7 @@ struct rsvdt_ctx {
   // rsvdt_rk4_steps: a second stream and an event for reading F3 back while
   // the last step's stages 2-4 run (created on first use).
   cudaStream_t io_stream = nullptr;
-  cudaEvent_t io_event = nullptr;
+  cudaEvent_t io_event = nullptr, up_event = nullptr;
   int64_t launches = 0;
   std::string err;
 
@@ -274,6 +274,8 @@ rsvdt_status launch_unforced_steps(rsvdt_ctx *ctx, int dir, z128 *cols, int64_t 
 int step_lanes(const rsvdt_ctx *ctx);
 bool use_cluster_engine(const rsvdt_ctx *ctx, int prec, int *C, int *threads);
 rsvdt_status run_last_step_split(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1);
+rsvdt_status launch_forcing_ahead(rsvdt_ctx *ctx, int dir, int prec, int64_t i);
+rsvdt_status launch_first_step_rest(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1);
 rsvdt_status debug_index_status(rsvdt_ctx *ctx);
 rsvdt_status launch_trans_steps(rsvdt_ctx *ctx, double dt, z128 *y, z128 *work, int64_t nsteps,
                                 cudaGraphExec_t *graph);

@@ -1268,6 +1268,72 @@ static rsvdt_status run_steps_cluster_t(rsvdt_ctx *ctx, int dir, int64_t i0, int
   return cuda_ok(ctx, cudaGetLastError(), "cluster steps") ? RSVDT_OK : RSVDT_ERR_CUDA;
 }
 
+// ------------------------------- first step with its forcing synthesised ahead
+//
+// rsvdt_rk4_steps uploads the state from host memory before its first step.
+// The step's forcing (F2, F3 from the slabs, the FP64 bulk of stage 1)
+// needs no state, so k_forcing_steps computes it while the upload is in
+// flight, and stage 1 then only adds the sparse product (k_stage1_pre):
+// the same operations in the same order as k_stage<Z, 1> (bit-identical).
+
+template <class Z>
+__global__ void __launch_bounds__(256) k_stage1_pre(const StepArgs<Z> P, const Z *__restrict__ fbuf) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t NK = P.N * P.K;
+  if (t >= NK) return;
+  const int64_t i = P.step[0];
+  if (t == 0) P.step[1] = i;
+  const int64_t n = t / P.K;
+  const int kc = (int)(t - n * P.K);
+  Z k = P.F3[t];  // the previous step's F3
+  row_product(P, n, kc, P.y, k);
+  const Z yv = P.y[t];
+  P.F2[t] = fbuf[t];
+  P.F3[t] = fbuf[NK + t];
+  P.zA[t] = zaxpy(P.dt_2, k, yv);
+  P.acc[t] = zaxpy(P.dt_6, k, yv);
+}
+
+template <class Z>
+static rsvdt_status forcing_ahead_t(rsvdt_ctx *ctx, int dir, int64_t i) {
+  auto P = make_args<Z>(ctx, dir, true);
+  const int64_t NK = P.N * P.K;
+  const size_t need = sizeof(Z) * 2 * (size_t)NK;
+  if (ctx->cl_bytes < need) {
+    dfree(ctx, ctx->cl_fbuf);
+    ctx->cl_fbuf = dalloc(ctx, need);
+    ctx->cl_bytes = ctx->cl_fbuf ? need : 0;
+    if (!ctx->cl_fbuf) return set_err(ctx, RSVDT_ERR_OOM, "forcing buffer allocation failed");
+  }
+  k_forcing_steps<Z><<<grid_for(NK, 256), 256, 0, ctx->stream>>>(P, i, 1, (Z *)ctx->cl_fbuf);
+  ctx->launches += 1;
+  return cuda_ok(ctx, cudaGetLastError(), "forcing") ? RSVDT_OK : RSVDT_ERR_CUDA;
+}
+
+template <class Z>
+static rsvdt_status first_step_rest_t(rsvdt_ctx *ctx, int dir, int64_t i, cudaEvent_t after_stage1) {
+  auto P = make_args<Z>(ctx, dir, true);
+  const int64_t NK = P.N * P.K;
+  k_set_step<<<1, 1, 0, ctx->stream>>>(ctx->d_step, i);
+  k_stage1_pre<Z><<<grid_for(NK, 256), 256, 0, ctx->stream>>>(P, (const Z *)ctx->cl_fbuf);
+  if (after_stage1) cudaEventRecord(after_stage1, ctx->stream);
+  for (int s = 2; s <= 4; ++s) launch_stage(s, P, ctx->stream);
+  ctx->launches += 5;
+  return cuda_ok(ctx, cudaGetLastError(), "first step") ? RSVDT_OK : RSVDT_ERR_CUDA;
+}
+
+// Step i's forcing into the forcing buffer (stream of the context).
+rsvdt_status launch_forcing_ahead(rsvdt_ctx *ctx, int dir, int prec, int64_t i) {
+  return prec == RSVDT_PREC_C64 ? forcing_ahead_t<z64>(ctx, dir, i) : forcing_ahead_t<z128>(ctx, dir, i);
+}
+
+// The rest of step i once the state is on the device: stage 1 from the
+// buffered forcing (after_stage1, if given, recorded after it), stages 2-4.
+rsvdt_status launch_first_step_rest(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1) {
+  return prec == RSVDT_PREC_C64 ? first_step_rest_t<z64>(ctx, dir, i, after_stage1)
+                                : first_step_rest_t<z128>(ctx, dir, i, after_stage1);
+}
+
 // Whether the cluster engine runs this context's steps (and its shape).
 bool use_cluster_engine(const rsvdt_ctx *ctx, int prec, int *C, int *threads) {
   if (ctx->engine == RSVDT_ENGINE_STAGES) return false;
