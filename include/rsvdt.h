@@ -237,12 +237,13 @@ int32_t rsvdt_get_lanes_per_row(const rsvdt_ctx *ctx);
 /* Stepping engine. STAGES: four stage launches per step (replayed from CUDA
  * graphs; lanes per row as above). CLUSTER (problems with at most 512 rows
  * x test vectors per SM of the cluster, 8192 for a cluster of 16): the
- * forcing of 64 steps at a time over the whole
- * GPU, then the 64 steps' stages on one thread-block cluster with a
- * hardware cluster barrier between stages, no launch per stage; the same
- * operations in the same order as the one-lane stage kernels
- * (bit-identical). AUTO (default) picks CLUSTER for problems of at most
- * 8192 values where the device can launch such a cluster. */
+ * forcing of 64 steps at a time over the whole GPU, then the 64 steps'
+ * stages on one thread-block cluster with a hardware cluster barrier
+ * between stages, no launch per stage; the same operations in the same
+ * order as the one-lane stage kernels (bit-identical). AUTO (default) picks
+ * CLUSTER for problems of at most 8192 values where the device can launch
+ * such a cluster; the lanes-per-row setting then applies only where the
+ * STAGES engine runs. */
 typedef enum { RSVDT_ENGINE_AUTO = 0, RSVDT_ENGINE_STAGES = 1, RSVDT_ENGINE_CLUSTER = 2 } rsvdt_step_engine;
 rsvdt_status rsvdt_set_step_engine(rsvdt_ctx *ctx, int32_t engine);
 int32_t rsvdt_get_step_engine(const rsvdt_ctx *ctx);
