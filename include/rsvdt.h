@@ -192,9 +192,11 @@ rsvdt_status rsvdt_get_results(rsvdt_ctx *ctx, double *U, int64_t ldu, double *V
  * starting at step index i0 (1-based, as SourceCode/TSRK4.c's i), with the
  * forcing built from the working block. Host state y (N x k, column-major,
  * complex) and F3 (forcing at the start of step i0, N x k) are read and
- * updated. For kernel-level tests and benchmarks; rsvdt_action is the
- * normal entry. Replaces SourceCode/TSRK4.c:6-51 called in the loop of
- * SourceCode/TSActionRK4.c:116-122. */
+ * updated (for the stage engine, the uploads run on a second stream while
+ * the first step's forcing is synthesised, and F3 is downloaded while the
+ * last step's stages 2-4 run). For kernel-level tests and benchmarks;
+ * rsvdt_action is the normal entry. Replaces SourceCode/TSRK4.c:6-51
+ * called in the loop of SourceCode/TSActionRK4.c:116-122. */
 rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps, double *y,
                              double *F3);
 
