@@ -150,6 +150,98 @@ def cpu_baseline(wl, g, Fk, steps: int, threads: int, warmup: int = 0):
     return float(np.mean(times))
 
 
+def parity_steps(wl, ctx, ctx64, threads: int, seed: int = 77):
+    """Parity at the benchmark's own size: two forced RK4 steps of all k test
+    vectors on the full operator through rsvdt_rk4_steps (host state, the
+    stage kernels the benchmark times: complex128 and the complex64
+    precision form) from a seeded state y0, F3_0 and the contexts' seeded
+    sketch, against the C restatement (SourceCode/TSRK4.c:18-47) on the same
+    inputs. The steps start at i0 = Ns, so the second one crosses the wrap
+    of the forcing index (jt = 2 Ns -> 0). Complex128 is checked in both
+    directions; the complex64 form (rounded state, FP32 arithmetic) against
+    the same complex128 oracle, where its error is the FP32 rounding."""
+    import oracle
+    import rsvdt
+    from rsvdt import synth
+
+    t0 = time.perf_counter()
+    g = ctx.grid()
+    F = ctx.get_block()
+    F64 = ctx64.get_block()
+    same_sketch = bool(np.array_equal(F, F64))
+    del F64
+    N, k = wl.N, wl.k
+    y0 = synth.complex_normal(N, k, seed)
+    F30 = synth.complex_normal(N, k, seed + 1)
+    A = synth.bcsr_to_csr(*wl.bcsr)
+    orc = oracle.Oracle(A, wl.Nw, wl.w, wl.dt_in, wl.transient_length)
+    orc.set_row_threads(threads)
+    i0, nsteps = g.Ns, 2
+    out = {"workload": f"{wl.name}: {nsteps} forced RK4 steps (i0 = Ns = {g.Ns}, across the forcing-index wrap) "
+                       f"of all k = {k} test vectors through rsvdt_rk4_steps, against the C restatement",
+           "same_sketch_in_both_contexts": same_sketch}
+    for name, c, d in (("c128_direct", ctx, rsvdt.DIRECT), ("c128_adjoint", ctx, rsvdt.ADJOINT),
+                       ("c64_direct", ctx64, rsvdt.DIRECT)):
+        y, F3 = c.rk4_steps(d, i0, nsteps, y0.copy(), F30.copy())
+        ey, ef = [], []
+        for ik in range(k):
+            Fk = np.asfortranarray(F[:, [iw * k + ik for iw in range(g.Nw_eff)]])
+            yo, F3o = orc.rk4_steps(d, Fk, i0, nsteps, y0[:, ik], F30[:, ik])
+            ey.append(float(np.linalg.norm(y[:, ik] - yo) / np.linalg.norm(yo)))
+            ef.append(float(np.linalg.norm(F3[:, ik] - F3o) / np.linalg.norm(F3o)))
+        out[name] = {"y_rel_err_max": max(ey), "F3_rel_err_max": max(ef)}
+    orc.close()
+    # Tolerances: complex128 1e-11 (the GPU's negative-frequency phasor is the
+    # exact conjugate of the positive one, the reference's is evaluated from
+    # a larger argument); complex64 1e-5 (FP32 rounding of the state, the
+    # operator, the forcing slabs and the sums, u = 6e-8, times the stage
+    # count and the cancellation in the products).
+    out["tolerance"] = {"c128": 1e-11, "c64": 1e-5}
+    out["pass"] = bool(same_sketch and all(out[n]["y_rel_err_max"] < 1e-11 and out[n]["F3_rel_err_max"] < 1e-11
+                                           for n in ("c128_direct", "c128_adjoint")) and
+                       out["c64_direct"]["y_rel_err_max"] < 1e-5 and out["c64_direct"]["F3_rel_err_max"] < 1e-5)
+    out["s"] = round(time.perf_counter() - t0, 1)
+    return out
+
+
+def parity_batch(fam, sketches, params, S_batched: dict, threads: int, q: int, count: int = 6):
+    """Parity of the batching form against the C restatement: `count` of
+    the batch's problems (the one where the complex64 batch is furthest
+    from the complex128 one, then the smallest ones, up to a row budget)
+    solved by the oracle's whole sequence (SourceCode/main.c:134-144) with
+    the batch's sketches, compared per gain with every batched form."""
+    import oracle
+
+    t0 = time.perf_counter()
+    worst = S_batched.get("worst_c64")
+    order = sorted(range(len(fam)), key=lambda i: fam[i]["N"] * fam[i]["k"] * fam[i]["Nw"])
+    pick = ([worst] if worst is not None else []) + [i for i in order if i != worst]
+    pick = pick[:count]
+    out = {"problems": [{"index": i, "N": fam[i]["N"], "k": fam[i]["k"], "Nw": fam[i]["Nw"]} for i in pick]}
+    errs = {name: [] for name in S_batched if name != "worst_c64"}
+    for i in pick:
+        pr = fam[i]
+        p = params(pr)
+        A = pr["A"]
+        if pr["beta"] > 0:
+            import scipy.sparse as sp
+            A = (A - pr["beta"] * sp.eye(A.shape[0], format="csr")).tocsr()
+        orc = oracle.Oracle(A, pr["Nw"], p.w, p.dt, p.TransientLength, threads=threads)
+        _, _, So = orc.run(sketches[i], q)
+        orc.close()
+        for name in errs:
+            Sb = S_batched[name][i]
+            errs[name].append((float((np.abs(Sb[:3] - So[:3]) / So[:3]).max()),
+                               float((np.abs(Sb - So) / So).max())))
+    for name, e in errs.items():
+        out[name] = {"gain_rel_err_max_j<=3": max(x[0] for x in e), "gain_rel_err_max": max(x[1] for x in e),
+                     "per_problem_j<=3": [x[0] for x in e]}
+    out["tolerance"] = {"batched_c128": 1e-9}
+    out["pass_c128"] = bool(out["batched_c128"]["gain_rel_err_max"] < 1e-9) if "batched_c128" in out else None
+    out["s"] = round(time.perf_counter() - t0, 1)
+    return out
+
+
 def time_to_gains(n: int, seed: int = 4321):
     """Full RSVD-Delta-t solve (SourceCode/main.c:134-144: direct action,
     q = 1 power iteration, SVDs, adjoint action) on the 3D operator of an
@@ -212,7 +304,7 @@ def time_to_gains(n: int, seed: int = 4321):
     return out
 
 
-def batch_form(count: int = 48, q: int = 0, seed: int = 2024):
+def batch_form(count: int = 48, q: int = 0, seed: int = 2024, parity_threads: int = 0):
     """Batching form: `count` Ginzburg-Landau problems (N log-uniform in
     [200, 20000], mu0 in [0.2, 0.45], k in {6, 10, 16}, Nw in {16, 32, 64};
     grid spacing of the 500-node case, dt = T/4096, one transient period,
@@ -220,7 +312,9 @@ def batch_form(count: int = 48, q: int = 0, seed: int = 2024):
     another in complex128 (the plain method, 48 sequential solves) and as
     one batch in complex128 and complex64. Wall time from the first action
     to every problem's gains on the host; each batch is run once untimed
-    first (autotuning, graph capture), then re-run on the same sketches."""
+    first (autotuning, graph capture), then re-run on the same sketches.
+    parity_threads > 0: also compares 6 of the problems with the C
+    restatement (parity_batch), returned under "parity"."""
     import rsvdt
     from rsvdt import synth
 
@@ -246,6 +340,7 @@ def batch_form(count: int = 48, q: int = 0, seed: int = 2024):
     out = {"workload": f"{count} Ginzburg-Landau problems, N {min(p['N'] for p in fam)}..{max(p['N'] for p in fam)} "
                        f"(log-uniform), k in {{6,10,16}}, Nw in {{16,32,64}}, dt = T/4096, q = {q}, seed {seed}",
            "sum_N_k": int(sum(p["N"] * p["k"] for p in fam)), "sequential_plain_c128_s": round(t_seq, 3)}
+    S_batched = {}
     for name, prec in (("batched_c128", rsvdt.PREC_C128), ("batched_c64", rsvdt.PREC_C64),
                        ("batched_c64_refine", rsvdt.PREC_C64_REFINE)):
         b = rsvdt.Batch(prec)
@@ -264,6 +359,9 @@ def batch_form(count: int = 48, q: int = 0, seed: int = 2024):
         err1 = [float((np.abs(Sb[0] - Ss[0]) / Ss[0]).max()) for Sb, Ss in zip(S_b, S_seq)]
         worst = int(np.argmax(errs))
         err = errs[worst]
+        S_batched[name] = S_b
+        if name == "batched_c64":
+            S_batched["worst_c64"] = worst
         th, lanes, ms = b.tuning()
         out[name + "_s"] = round(t_b, 3)
         out[name + "_speedup_vs_sequential"] = round(t_seq / t_b, 3)
@@ -277,6 +375,9 @@ def batch_form(count: int = 48, q: int = 0, seed: int = 2024):
         out[name + "_tuned"] = {"threads": th, "lanes_per_row": lanes, "values_per_lane": b.values_per_lane(),
                                 "ms_per_batched_step": round(ms, 4)}
         b.close()
+    if parity_threads:
+        out["parity"] = parity_batch(fam, sketches, lambda pr: params(pr, rsvdt.PREC_C128), S_batched,
+                                     parity_threads, q)
     return out
 
 
@@ -501,9 +602,11 @@ def run_reference(args):
     if rank != 0:
         return
     from rsvdt import workloads
-    # The per-step work does not depend on the operator's diagonal shift:
-    # the host-only shift estimate keeps this arm off the GPU.
-    wl = workloads.make_3d(n=args.n, shift="local")
+    # The recorded shift builds the same operator as the GPU arm without a
+    # GPU; for a grid with no recorded shift the host-only estimate stands
+    # in (the per-step work does not depend on the diagonal shift).
+    known = (args.n, 7) in workloads.RECORDED_GROWTH_RATE
+    wl = workloads.make_3d(n=args.n, shift="recorded" if known else "local")
     import oracle
     dt, Ns, Nt, R = oracle.setup_grid(wl.w, wl.Nw, wl.dt_in, wl.transient_length)
     Fk = np.asfortranarray(np.random.default_rng(1).standard_normal((wl.N, wl.Nw)) + 0j)
@@ -536,6 +639,7 @@ def main():
     ap.add_argument("--no-ttg", action="store_true", help="skip the time-to-gains solves")
     ap.add_argument("--no-batch", action="store_true", help="skip the batching-form comparison")
     ap.add_argument("--no-gl1", action="store_true", help="skip the 500-node Ginzburg-Landau runs")
+    ap.add_argument("--no-parity", action="store_true", help="skip the at-size parity checks against the oracle")
     ap.add_argument("--learned", action="store_true", help="run the learned-sketch experiment (about a minute)")
     ap.add_argument("--learned3d", action="store_true", help="run the 3D learned-sketch experiment (a few minutes)")
     ap.add_argument("--ttg-n", type=int, default=64, help="grid of the time-to-gains solves")
@@ -633,17 +737,32 @@ def main():
     ctx64.rk4_reset(rsvdt.DIRECT)
     ctx64.rk4_advance(rsvdt.DIRECT, 1, 3)
     ms64 = timed(ctx64, 4, args.steps) / args.steps
-    b64 = wl.step_bytes(g.ResRatio, s_c=8)
-    st64 = [x / nprof for x in ctx64.rk4_profile(rsvdt.DIRECT, 4 + args.steps, nprof)]
-    ctx64.close()
+    fb64 = ctx64.forcing_block()
+    b64 = wl.step_bytes(g.ResRatio, s_c=8, forcing_block=fb64)
+    # Per-kernel times over 2 forcing blocks (32 steps), per step.
+    nprof64 = 2 * max(fb64, 1) if fb64 else nprof
+    st64 = [x / nprof64 for x in ctx64.rk4_profile_ex(rsvdt.DIRECT, 4 + args.steps, nprof64)]
+    # The same step with stage 1 synthesising every step's forcing (the
+    # form before the forcing block), for comparison.
+    ctx64.set_forcing_block(0)
+    ctx64.rk4_advance(rsvdt.DIRECT, 4 + args.steps + nprof64, 3)
+    ms64_nofb = timed(ctx64, 7 + args.steps + nprof64, args.steps) / args.steps
+    ctx64.set_forcing_block(-1)
     torch.cuda.nvtx.range_pop()
 
+    threads = os.cpu_count() or 1
+    parity = {}
+    if rank == 0 and not args.no_parity:
+        parity["steps_" + wl.name] = parity_steps(wl, ctx, ctx64, threads)
+    ctx64.close()
     ttg = None
     if rank == 0 and not args.no_ttg:
         ttg = time_to_gains(args.ttg_n)
     batching = None
     if rank == 0 and not args.no_batch:
-        batching = batch_form()
+        batching = batch_form(parity_threads=0 if args.no_parity else threads)
+        if "parity" in batching:
+            parity["batch"] = batching.pop("parity")
     learned_res = None
     if rank == 0 and args.learned:
         learned_res = learned_form()
@@ -660,12 +779,29 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         Fk = np.asfortranarray(np.random.default_rng(1).standard_normal((wl.N, wl.Nw)) + 0j)
-        threads = os.cpu_count() or 1
         t_cpu = cpu_baseline(wl, g, Fk, 2, threads)
         cpu = {"value": round(b["step"] / t_cpu / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                "sample": f"2 steps x {wl.k} test vectors of the same 3D64 step, row loops on {threads} threads "
                          f"({t_cpu:.2f} s/step); C restatement of SourceCode/TSRK4.c"}
     ctx.close()
+
+    def gbs(nbytes, ms):
+        return nbytes / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+
+    c64 = {"ms_per_step": round(ms64, 4), "forcing_block_steps": fb64,
+           "value": round(gbs(b64["step"], ms64), 3), "unit": "GB/s", "frac": round(gbs(b64["step"], ms64) / hbm, 4),
+           "step_bytes": b64["step"],
+           "stage_ms": [round(x, 4) for x in st64[:4]], "forcing_block_ms": round(st64[4], 4),
+           "kernels": "k_forcing_block<32,pair> + k_bstage<z64,10,2,1..4,FB> (lane groups per 5x5 block row)",
+           "forcing_gbs": round(gbs(b64["forcing"], st64[4]), 2),
+           "forcing_frac": round(gbs(b64["forcing"], st64[4]) / hbm, 4),
+           "stage1_gbs": round(gbs(b64["stage1"], st64[0]), 2),
+           "stage1_frac": round(gbs(b64["stage1"], st64[0]) / hbm, 4),
+           "stage2_gbs": round(gbs(b64["stage234"], st64[1]), 2),
+           "stage2_frac": round(gbs(b64["stage234"], st64[1]) / hbm, 4),
+           "stage4_gbs": round(gbs(b64["stage4"], st64[3]), 2),
+           "ms_per_step_without_forcing_block": round(ms64_nofb, 4),
+           "speedup_vs_c128": round(ms_step / ms64, 3)}
 
     if rank == 0:
         out = {
@@ -682,20 +818,18 @@ def main():
                          "traffic": round(8.8219e9 * wl.N / 1310720),
                          "traffic_source": "ncu dram__bytes_read+write of k_rstage<z128,10,1> at 3D64, one launch",
                          "bytes_per_launch": b["stage1"], "ms_per_launch": round(st_ms[0], 4),
+                         "fp64_frac": round(ach_fp64 / fp64_peak, 4),
+                         # The precision form's step (complex64 stages, forcing block) on the
+                         # same operator, against the same HBM peak.
+                         "c64_ms_per_step": c64["ms_per_step"], "c64_step_frac": c64["frac"],
+                         "c64_forcing_frac": c64["forcing_frac"], "c64_stage1_frac": c64["stage1_frac"],
+                         "c64_stage2_frac": c64["stage2_frac"],
                          "fp64": {"achieved_tflops": round(ach_fp64, 4), "peak_tflops": round(fp64_peak, 4),
                                   "frac": round(ach_fp64 / fp64_peak, 4),
                                   "note": "plain complex128 form is FP64-bound on GB300; peak = cuBLAS DGEMM"}},
             "stage_ms": [round(x, 4) for x in st_ms],
             "step_fp64_tflops": round(step_fp64, 4),
-            "precision_form_c64": {"ms_per_step": round(ms64, 4),
-                                   "value": round(b64["step"] / (ms64 * 1e-3) / 1e9, 3), "unit": "GB/s",
-                                   "frac": round(b64["step"] / (ms64 * 1e-3) / 1e9 / hbm, 4),
-                                   "stage_ms": [round(x, 4) for x in st64],
-                                   "kernels": "k_bstage<z64,10,2,1..4> (lane groups per 5x5 block row)",
-                                   "stage1_gbs": round(b64["stage1"] / (st64[0] * 1e-3) / 1e9, 2),
-                                   "stage1_frac": round(b64["stage1"] / (st64[0] * 1e-3) / 1e9 / hbm, 4),
-                                   "stage234_gbs": round(b64["stage234"] / (st64[1] * 1e-3) / 1e9, 2),
-                                   "speedup_vs_c128": round(ms_step / ms64, 3)},
+            "precision_form_c64": c64,
             "clocks": clk,
             "gpu_launches": int(launches),
             "e2e": {"value": round(b["step"] / e2e_t / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": io_bytes,
@@ -708,6 +842,7 @@ def main():
             "learned_sketch_3d": learned3d,
             "gl1": gl1,
             "precision_form_large": large,
+            "parity": parity or None,
         }
         print(json.dumps(out))
     if dist:

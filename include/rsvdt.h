@@ -194,7 +194,9 @@ rsvdt_status rsvdt_get_results(rsvdt_ctx *ctx, double *U, int64_t ldu, double *V
  * complex) and F3 (forcing at the start of step i0, N x k) are read and
  * updated (for the stage engine, the uploads run on a second stream while
  * the first step's forcing is synthesised, and F3 is downloaded while the
- * last step's stages 2-4 run). For kernel-level tests and benchmarks;
+ * last step's stages 2-4 run). In the precision form (RSVDT_PREC_C64) the
+ * host values are rounded to complex64 on upload and widened back on
+ * download. For kernel-level tests and benchmarks;
  * rsvdt_action is the normal entry. Replaces SourceCode/TSRK4.c:6-51
  * called in the loop of SourceCode/TSActionRK4.c:116-122. */
 rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps, double *y,
@@ -209,9 +211,31 @@ rsvdt_status rsvdt_rk4_advance(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_
 /* Runs nsteps device-resident steps (as rsvdt_rk4_advance) launching the
  * four RK4 stage kernels one by one with CUDA events between them on the
  * context's stream; stage_ms[0..3] receive each stage's total time in
- * milliseconds. For benchmarks and roofline measurements. */
+ * milliseconds (stage 1 including the forcing-block kernel when the forcing
+ * is synthesised ahead, see rsvdt_set_forcing_block). For benchmarks and
+ * roofline measurements. */
 rsvdt_status rsvdt_rk4_profile(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps,
                                double *stage_ms);
+/* As rsvdt_rk4_profile, with the forcing-block kernel timed on its own:
+ * times_ms[0..3] the four stages, times_ms[4] the forcing-block launches (0
+ * when stage 1 synthesises the forcing). */
+rsvdt_status rsvdt_rk4_profile_ex(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps,
+                                  double *times_ms);
+
+/* Forcing synthesis of the complex64 block-row stages (5x5 block-CSR
+ * operator, k in {2, 4, 6, 8, 10, 16}, Nw_eff in {8, 16, 32, 64}): the
+ * forcing at the two times of each step (SourceCode/CreateForcingOnFly.c:
+ * 17-19, called twice per step by SourceCode/TSRK4.c:21-27) is a sum over
+ * the Nw_eff frequency coefficients of each (row, test vector). steps = 0:
+ * stage 1 forms it every step, reading all the coefficients every step.
+ * steps = G (1, 2, 4, 8 or 16): one kernel forms the forcings of G steps at
+ * once, reading the coefficients once per G steps, into a buffer of
+ * 2 G N k complex64 values that stages 1-4 read (same operations in the same
+ * order: identical results). -1 (default): 16 when the buffer fits with 4
+ * GiB of device memory to spare, else 0. Other stage kernels ignore it. */
+rsvdt_status rsvdt_set_forcing_block(rsvdt_ctx *ctx, int32_t steps);
+/* Block length in use by the last complex64 stepping (0 = none). */
+int32_t rsvdt_get_forcing_block(const rsvdt_ctx *ctx);
 
 /* ----------------------------------------------------------- capacity mode
  * For problems whose spectral blocks do not fit several times in device
@@ -410,19 +434,30 @@ rsvdt_status rsvdt_mlp_train(rsvdt_mlp *n, const float *X, const float *T, int64
  * x k complex128 values in the library's spectral-block layout
  * Y[(row*nw + iw)*k + j]; Q may equal Y. Each row-frequency block is
  * orthonormalised with the same shifted CholQR passes as
- * rsvdt_qr_all_freqs, on `stream` (a cudaStream_t; NULL is the legacy
- * default stream), and the call returns after the stream has finished
- * this work.
+ * rsvdt_qr_all_freqs, on `stream` (a cudaStream_t), and the call returns
+ * after the stream has finished this work (it waits for a 4-byte status
+ * read back into host memory).
+ *
+ * Stream: NULL is the legacy default stream, which synchronises with every
+ * blocking stream of the device; while another stream is being captured
+ * that implicit synchronisation invalidates the capture. Callers in that
+ * situation must pass a non-blocking stream of their own
+ * (cudaStreamNonBlocking) or cudaStreamPerThread.
  *
  * Scratch comes from a fixed 4 MiB device array inside the library, one
- * per GPU that loads it, held until the process exits. Limits: k <= 32 and
- * nw*k*k <= 65535; larger sizes return RSVDT_ERR_ARG without touching the
- * GPU. The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * Every call reuses the same array, so calls that overlap on the GPU (from
- * two streams or two host threads at once) race and must be serialised by
- * the caller. errbuf (optional, errlen bytes) receives a message on
- * failure. */
+ * per device context that loads the library's device code, held as long as
+ * that context lives (until the process exits, or until the context is torn
+ * down, e.g. by cudaDeviceReset). Limits: k <= 32 and nw*k*k <= 65535;
+ * larger sizes return RSVDT_ERR_ARG without touching the GPU. Every call
+ * looks up the array's device address in the current context
+ * (cudaGetSymbolAddress, a host-side query that allocates nothing); the
+ * first call in a context may load the library's device code, so make that
+ * first call before any stream capture. Every call reuses the same array,
+ * so calls that overlap on the GPU (from two streams or two host threads at
+ * once) race and must be serialised by the caller. The Gram products form
+ * the full k x k matrices (twice the work of rsvdt_qr_all_freqs, which forms
+ * one triangle); the QR stages are a small part of a solve. errbuf
+ * (optional, errlen bytes) receives a message on failure. */
 rsvdt_status rsvdt_qr_all_freqs_noalloc(const double *Y, double *Q, int64_t rows, int64_t nw,
                                         int64_t k, void *stream, char *errbuf, int64_t errlen);
 

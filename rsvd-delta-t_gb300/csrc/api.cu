@@ -672,7 +672,7 @@ rsvdt_status rsvdt_create(const rsvdt_params *p, rsvdt_ctx **out) {
       st = RSVDT_ERR_CUDA;
   }
   if (st == RSVDT_OK) {
-    ctx->d_step = (int64_t *)dalloc(ctx, sizeof(int64_t) * 2);
+    ctx->d_step = (int64_t *)dalloc(ctx, sizeof(int64_t) * 4);
     ctx->d_flags = (int32_t *)dalloc(ctx, sizeof(int32_t) * 4);
     if (!ctx->d_step || !ctx->d_flags) st = set_err(ctx, RSVDT_ERR_OOM, "device allocation failed");
   }
@@ -1236,10 +1236,32 @@ rsvdt_status rsvdt_rk4_advance(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_
   return run_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, ctx->act_prec, i0, nsteps, true);
 }
 
-rsvdt_status rsvdt_rk4_profile(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps, double *stage_ms) {
+rsvdt_status rsvdt_rk4_profile_ex(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps, double *times_ms) {
   RSVDT_TRY(require_ready(ctx, true));
-  if (i0 < 1 || nsteps < 1 || !stage_ms) return set_err(ctx, RSVDT_ERR_ARG, "invalid profile arguments");
-  return profile_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, ctx->act_prec, i0, nsteps, stage_ms);
+  if (i0 < 1 || nsteps < 1 || !times_ms) return set_err(ctx, RSVDT_ERR_ARG, "invalid profile arguments");
+  return profile_steps(ctx, dir == RSVDT_DIRECT ? 1 : 0, ctx->act_prec, i0, nsteps, times_ms);
+}
+
+rsvdt_status rsvdt_rk4_profile(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps, double *stage_ms) {
+  if (!stage_ms) return set_err(ctx, RSVDT_ERR_ARG, "invalid profile arguments");
+  double t[5] = {0, 0, 0, 0, 0};
+  RSVDT_TRY(rsvdt_rk4_profile_ex(ctx, dir, i0, nsteps, t));
+  stage_ms[0] = t[0] + t[4];  // the forcing block replaces stage 1's synthesis
+  for (int s = 1; s < 4; ++s) stage_ms[s] = t[s];
+  return RSVDT_OK;
+}
+
+rsvdt_status rsvdt_set_forcing_block(rsvdt_ctx *ctx, int32_t steps) {
+  if (!ctx) return RSVDT_ERR_ARG;
+  if (steps != -1 && steps != 0 && steps != 1 && steps != 2 && steps != 4 && steps != 8 && steps != 16)
+    return set_err(ctx, RSVDT_ERR_ARG, "forcing block of %d steps (allowed: -1, 0, 1, 2, 4, 8, 16)", (int)steps);
+  ctx->fb_steps = steps;
+  return RSVDT_OK;
+}
+
+int32_t rsvdt_get_forcing_block(const rsvdt_ctx *ctx) {
+  if (!ctx) return 0;
+  return ctx->fb_last;
 }
 
 rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t nsteps, double *y, double *F3) {
@@ -1248,8 +1270,6 @@ rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t 
   if (ctx->capacity) return set_err(ctx, RSVDT_ERR_STATE, "rsvdt_rk4_steps is not available in capacity mode");
   if (ctx->blk_rows != ctx->N) return set_err(ctx, RSVDT_ERR_STATE, "working block must have N rows");
   const int prec = ctx->act_prec;
-  if (prec == RSVDT_PREC_C64)
-    return set_err(ctx, RSVDT_ERR_ARG, "rsvdt_rk4_steps reads back complex128 state only");
   const int64_t N = ctx->N, K = ctx->K;
   ctx->Nstore = ctx->par.TransientRemoval ? ctx->Nw + 1 : ctx->Nw;
   RSVDT_TRY(stage_forcing_cached(ctx, prec));
@@ -1266,7 +1286,21 @@ rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t 
   const size_t bytes = sizeof(z128) * (size_t)N * K;
   const int d = dir == RSVDT_DIRECT ? 1 : 0;
   int C = 0, cth = 0;
-  if (nsteps >= 1 && step_lanes(ctx) == 1 && !use_cluster_engine(ctx, prec, &C, &cth)) {
+  if (prec == RSVDT_PREC_C64) {
+    // Precision form: the complex128 host state is rounded to complex64 on
+    // the way in and widened on the way out.
+    if (!cuda_ok(ctx, cudaMemcpyAsync(sy, y, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload") ||
+        !cuda_ok(ctx, cudaMemcpyAsync(sf, F3, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload"))
+      return RSVDT_ERR_CUDA;
+    RSVDT_TRY(launch_colmajor_to_blk64(ctx, sy, N, N, K, (z64 *)ctx->y));
+    RSVDT_TRY(launch_colmajor_to_blk64(ctx, sf, N, N, K, (z64 *)ctx->F3));
+    RSVDT_TRY(run_steps(ctx, d, prec, i0, nsteps, true));
+    RSVDT_TRY(launch_blk64_to_colmajor(ctx, (const z64 *)ctx->y, N, K, sy, N));
+    RSVDT_TRY(launch_blk64_to_colmajor(ctx, (const z64 *)ctx->F3, N, K, sf, N));
+    if (!cuda_ok(ctx, cudaMemcpyAsync(y, sy, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download") ||
+        !cuda_ok(ctx, cudaMemcpyAsync(F3, sf, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download"))
+      return RSVDT_ERR_CUDA;
+  } else if (nsteps >= 1 && step_lanes(ctx) == 1 && !use_cluster_engine(ctx, prec, &C, &cth)) {
     if (!ctx->io_stream &&
         (!cuda_ok(ctx, cudaStreamCreateWithFlags(&ctx->io_stream, cudaStreamNonBlocking), "stream create") ||
          !cuda_ok(ctx, cudaEventCreateWithFlags(&ctx->io_event, cudaEventDisableTiming), "event create") ||

@@ -203,6 +203,16 @@ struct rsvdt_ctx {
   // step_lanes): lanes per row (0 = chosen from the size), the argument
   // blocks of both directions, the work list and the cached graphs.
   int lanes_override = 0;
+  // Forcing blocks of the complex64 block-row stages (rsvdt_set_forcing_block:
+  // -1 = automatic, 0 = synthesised in stage 1, else the block length),
+  // their buffer, and the block length each cached step graph was captured
+  // with.
+  int fb_steps = -1;
+  void *fblk = nullptr;
+  size_t fb_bytes = 0;
+  int step_graph_fb[2] = {-1, -1};
+  int fb_last = 0;  // block length of the last complex64 stepping (0: none)
+  int sm_count = 0;
   // rsvdt_step_engine, and the cluster engine's forcing buffer.
   int engine = RSVDT_ENGINE_AUTO;
   void *cl_fbuf = nullptr;
@@ -259,6 +269,8 @@ rsvdt_status stage_forcing_coeffs(rsvdt_ctx *ctx, int prec);
 rsvdt_status launch_forcing_init(rsvdt_ctx *ctx, int dir, int prec);
 rsvdt_status run_steps(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_t nsteps,
                        bool sample);
+// stage_ms[0..3]: the four stages; stage_ms[4]: the forcing-block kernel
+// (0 when stage 1 synthesises the forcing).
 rsvdt_status profile_steps(rsvdt_ctx *ctx, int dir, int prec, int64_t i0, int64_t nsteps,
                            double *stage_ms);
 rsvdt_status launch_dft(rsvdt_ctx *ctx, int prec, z128 *out);
@@ -284,6 +296,13 @@ rsvdt_status launch_colmajor_to_blk(rsvdt_ctx *ctx, const z128 *src, int64_t row
                                     int64_t C, z128 *dst);
 rsvdt_status launch_blk_to_colmajor(rsvdt_ctx *ctx, const z128 *src, int64_t rows, int64_t C,
                                     z128 *dst, int64_t ld, cudaStream_t st = nullptr);
+// Complex64 state <-> complex128 host layout (rsvdt_rk4_steps in the
+// precision form): the same transposes, rounding to / widening from
+// complex64.
+rsvdt_status launch_colmajor_to_blk64(rsvdt_ctx *ctx, const z128 *src, int64_t rows, int64_t ld,
+                                      int64_t C, z64 *dst);
+rsvdt_status launch_blk64_to_colmajor(rsvdt_ctx *ctx, const z64 *src, int64_t rows, int64_t C,
+                                      z128 *dst, int64_t ld);
 rsvdt_status apply_weight(rsvdt_ctx *ctx, const DevCSR &M, const z128 *in, z128 *out,
                           int64_t C);
 rsvdt_status cholqr2(rsvdt_ctx *ctx, z128 *blk, int64_t rows, int64_t nw, int64_t K,

@@ -57,6 +57,44 @@ __global__ void k_row_to_col(const z128 *__restrict__ src, int64_t rows, int64_t
   }
 }
 
+// Complex64 variants: dst[r][c] = (complex64) src[c*ld + r], and
+// dst[c*ld + r] = (complex128) src[r][c].
+__global__ void k_col_to_row_c64(const z128 *__restrict__ src, int64_t rows, int64_t ld, int64_t C,
+                                 z64 *__restrict__ dst) {
+  __shared__ z128 tile[32][33];
+  const int64_t r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    int64_t c = c0 + j, r = r0 + threadIdx.x;
+    if (c < C && r < rows) tile[j][threadIdx.x] = src[c * ld + r];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    int64_t r = r0 + j, c = c0 + threadIdx.x;
+    if (c < C && r < rows) {
+      const z128 v = tile[threadIdx.x][j];
+      dst[r * C + c] = zmake<z64>((float)v.re, (float)v.im);
+    }
+  }
+}
+
+__global__ void k_row_to_col_c64(const z64 *__restrict__ src, int64_t rows, int64_t C,
+                                 z128 *__restrict__ dst, int64_t ld) {
+  __shared__ z64 tile[32][33];
+  const int64_t r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    int64_t r = r0 + j, c = c0 + threadIdx.x;
+    if (c < C && r < rows) tile[j][threadIdx.x] = src[r * C + c];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    int64_t c = c0 + j, r = r0 + threadIdx.x;
+    if (c < C && r < rows) {
+      const z64 v = tile[threadIdx.x][j];
+      dst[c * ld + r] = zmake<z128>((double)v.re, (double)v.im);
+    }
+  }
+}
+
 static dim3 tgrid(int64_t rows, int64_t C) {
   return dim3((unsigned)((rows + 31) / 32), (unsigned)((C + 31) / 32));
 }
@@ -73,6 +111,22 @@ rsvdt_status launch_blk_to_colmajor(rsvdt_ctx *ctx, const z128 *src, int64_t row
                                     z128 *dst, int64_t ld, cudaStream_t st) {
   if ((C + 31) / 32 > 65535) return set_err(ctx, RSVDT_ERR_ARG, "too many columns (%lld)", (long long)C);
   k_row_to_col<<<tgrid(rows, C), dim3(32, 8), 0, st ? st : ctx->stream>>>(src, rows, C, dst, ld);
+  ctx->launches += 1;
+  return cuda_ok(ctx, cudaGetLastError(), "transpose") ? RSVDT_OK : RSVDT_ERR_CUDA;
+}
+
+rsvdt_status launch_colmajor_to_blk64(rsvdt_ctx *ctx, const z128 *src, int64_t rows, int64_t ld,
+                                      int64_t C, z64 *dst) {
+  if ((C + 31) / 32 > 65535) return set_err(ctx, RSVDT_ERR_ARG, "too many columns (%lld)", (long long)C);
+  k_col_to_row_c64<<<tgrid(rows, C), dim3(32, 8), 0, ctx->stream>>>(src, rows, ld, C, dst);
+  ctx->launches += 1;
+  return cuda_ok(ctx, cudaGetLastError(), "transpose") ? RSVDT_OK : RSVDT_ERR_CUDA;
+}
+
+rsvdt_status launch_blk64_to_colmajor(rsvdt_ctx *ctx, const z64 *src, int64_t rows, int64_t C,
+                                      z128 *dst, int64_t ld) {
+  if ((C + 31) / 32 > 65535) return set_err(ctx, RSVDT_ERR_ARG, "too many columns (%lld)", (long long)C);
+  k_row_to_col_c64<<<tgrid(rows, C), dim3(32, 8), 0, ctx->stream>>>(src, rows, C, dst, ld);
   ctx->launches += 1;
   return cuda_ok(ctx, cudaGetLastError(), "transpose") ? RSVDT_OK : RSVDT_ERR_CUDA;
 }
@@ -915,12 +969,8 @@ namespace {
 
 constexpr size_t kNoAllocScratchBytes = 4u << 20;  // 4 MiB
 constexpr size_t kNoAllocElems = kNoAllocScratchBytes / sizeof(rsvdt::z128);
-constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) rsvdt::z128 g_noalloc_scratch[kNoAllocElems];
-
-// Device address of g_noalloc_scratch, looked up once per device.
-static void *g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
 
 // Gram partials with a caller-chosen chunk length (variant of k_gram_part,
 // which uses a fixed chunk of kGramRows rows).
@@ -990,21 +1040,19 @@ extern "C" rsvdt_status rsvdt_qr_all_freqs_noalloc(const double *Y, double *Q, i
                         "nw*k*k = %lld needs %lld bytes of scratch; the fixed scratch array holds %zu bytes "
                         "(limit nw*k*k <= %lld)",
                         (long long)pk, (long long)(4 * pk + 1) * 16, kNoAllocScratchBytes, (long long)(avail / 4));
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
-    return noalloc_fail(errbuf, errlen, RSVDT_ERR_CUDA, "no usable current CUDA device (%s)", cudaGetErrorString(e));
-  if (!g_noalloc_ptr[dev]) {
-    // First call on this device: look up the array's device address (a host
-    // symbol's address is not a device address).
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return noalloc_fail(errbuf, errlen, RSVDT_ERR_CUDA, "cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = p;
-  }
+  // The array's device address in the current device's context. It is
+  // looked up on every call rather than cached: after a cudaDeviceReset (or
+  // any other teardown of the context) the module is loaded again and the
+  // array can sit at a new address. The lookup is a host-side query and
+  // allocates nothing; only the first call in a context may load the
+  // library's device code into it. A host symbol's address is not a device
+  // address, so the kernels get this pointer, never &g_noalloc_scratch.
+  void *scr_ptr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&scr_ptr, g_noalloc_scratch);
+  if (e != cudaSuccess || !scr_ptr)
+    return noalloc_fail(errbuf, errlen, RSVDT_ERR_CUDA, "cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
   cudaStream_t s = (cudaStream_t)stream;
-  z128 *scr = (z128 *)g_noalloc_ptr[dev];
+  z128 *scr = (z128 *)scr_ptr;
   int64_t chunks = std::min((rows + kGramRows - 1) / kGramRows, avail / pk - 3);
   if (chunks < 1) chunks = 1;
   const int64_t chunk_rows = (rows + chunks - 1) / chunks;

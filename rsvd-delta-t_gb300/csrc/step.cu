@@ -40,6 +40,8 @@
 // k_stage_batched_pair (two complex64 test vectors per lane). Stage
 // kernels are launched with programmatic dependent launch. This file also
 // holds the DFT of the sampled period (radix-2 FFT for Nw = 8..64).
+#include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstring>
 
@@ -64,6 +66,11 @@ struct StepArgs {
   typename real_of<Z>::type dt, dt_2, dt_6, dt_62;  // dt, dt/2, dt/6, dt/6*2
   int64_t *step;
   int64_t rend;  // last step of this problem's action (batched stepping)
+  // Forcing block (complex64 block-row stages only): the half-step forcings
+  // of a block of steps, synthesised ahead by k_forcing_block, slot 2s at
+  // the half step and 2s+1 at the end of the block's step s; nullptr when
+  // stage 1 synthesises each step's forcing itself.
+  Z *fblk;
 };
 
 // Programmatic dependent launch: a stage kernel is launched while the one
@@ -347,8 +354,15 @@ static const int kRowThreads = 128;
 // flight for their latency-bound gathers (measured faster on the 64^3
 // operator than the unbounded 108-register build); stage 1 keeps its
 // registers for the forcing synthesis.
-template <class Z, int K, int KP, int S>
-__global__ void __launch_bounds__(kRowThreads, S == 1 ? 1 : 8) k_bstage(const StepArgs<Z> P) {
+//
+// FB (forcing block, P.fblk): the forcings were synthesised ahead for a
+// block of steps (k_forcing_block, which recorded the block's first step in
+// step[2] and its length in step[3]); step s of the block adds slot 2s-1
+// (s > 0; the state F3 for s = 0) in stage 1, slot 2s in stages 2 and 3 and
+// slot 2s+1 in stage 4, and the block's last step writes its end forcing
+// to the state F3. Stage 1 then neither synthesises nor writes F2 / F3.
+template <class Z, int K, int KP, int S, bool FB = false>
+__global__ void __launch_bounds__(kRowThreads, (S == 1 && !FB) ? 1 : 8) k_bstage(const StepArgs<Z> P) {
   pdl_wait_and_release();
   constexpr int L = K / KP;
   constexpr int BPW = 32 / L;
@@ -360,6 +374,103 @@ __global__ void __launch_bounds__(kRowThreads, S == 1 ? 1 : 8) k_bstage(const St
   const int sub = lane / L, q = lane - sub * L;
   const int64_t br = warp * BPW + sub;
   const int64_t i = (S == 1) ? P.step[0] : P.step[1];
+  if constexpr (FB) {
+    if (br >= P.N / 5 || sub >= BPW) return;
+    if (S == 1 && br == 0 && q == 0) P.step[1] = i;
+    const int64_t NK = P.N * K;
+    const int64_t sb = i - P.step[2];  // step of the block, 0 .. step[3]-1
+    const int64_t base = br * 5 * K + q * KP;
+    const Z *x = (S == 1) ? P.y : (S == 2) ? P.zA : (S == 3) ? P.zB : P.zA;
+    const Z *addv = (S == 1)   ? (sb == 0 ? P.F3 : P.fblk + (2 * sb - 1) * NK)
+                    : (S == 4) ? P.fblk + (2 * sb + 1) * NK
+                               : P.fblk + 2 * sb * NK;
+    Z k[5][KP];
+#pragma unroll
+    for (int r = 0; r < 5; ++r) ldg_chunk<Z, KP>(addv + base + r * K, k[r]);
+    if (S == 4 && sb == P.step[3] - 1) {
+#pragma unroll
+      for (int r = 0; r < 5; ++r) st_chunk<Z, KP>(P.F3 + base + r * K, k[r]);
+    }
+    const int32_t b = __ldg(P.rowptr + br), e = __ldg(P.rowptr + br + 1);
+    for (int32_t j = b; j < e; ++j) {
+      const int32_t cb = __ldg(P.col + j);
+      if (!RSVDT_CHECK_INDEX(cb >= 0 && cb < P.N / 5, 1)) continue;
+      const int64_t c0 = (int64_t)cb * 5;
+      const Z *blk = P.val + (int64_t)j * P.bstride;
+      if constexpr (S == 4 && sizeof(Z) == 8) {
+        // The padded 26-value block as 13 aligned 16-byte loads.
+        Z a[26];
+        const float4 *b4 = reinterpret_cast<const float4 *>(blk);
+#pragma unroll
+        for (int m = 0; m < 13; ++m) {
+          const float4 t = __ldg(b4 + m);
+          a[2 * m] = zmake<Z>(t.x, t.y);
+          a[2 * m + 1] = zmake<Z>(t.z, t.w);
+        }
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+          Z xv[KP];
+          ldg_chunk<Z, KP>(x + (c0 + c) * K + q * KP, xv);
+#pragma unroll
+          for (int r = 0; r < 5; ++r)
+#pragma unroll
+            for (int p = 0; p < KP; ++p) zmac(k[r][p], a[r * 5 + c], xv[p]);
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+          Z xv[KP];
+          ldg_chunk<Z, KP>(x + (c0 + c) * K + q * KP, xv);
+#pragma unroll
+          for (int r = 0; r < 5; ++r) {
+            const Z a = blk[r * 5 + c];
+#pragma unroll
+            for (int p = 0; p < KP; ++p) zmac(k[r][p], a, xv[p]);
+          }
+        }
+      }
+    }
+    if (S == 1) {
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        Z yv[KP], t[KP];
+        ldg_chunk<Z, KP>(P.y + base + r * K, yv);
+#pragma unroll
+        for (int p = 0; p < KP; ++p) t[p] = zaxpy(P.dt_2, k[r][p], yv[p]);
+        st_chunk<Z, KP>(P.zA + base + r * K, t);
+#pragma unroll
+        for (int p = 0; p < KP; ++p) t[p] = zaxpy(P.dt_6, k[r][p], yv[p]);
+        st_chunk<Z, KP>(P.acc + base + r * K, t);
+      }
+    } else if (S == 2 || S == 3) {
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        Z yv[KP], t[KP], av[KP];
+        ldg_chunk<Z, KP>(P.y + base + r * K, yv);
+#pragma unroll
+        for (int p = 0; p < KP; ++p) t[p] = zaxpy(S == 2 ? P.dt_2 : P.dt, k[r][p], yv[p]);
+        st_chunk<Z, KP>((S == 2 ? P.zB : P.zA) + base + r * K, t);
+        ld_chunk<Z, KP>(P.acc + base + r * K, av);
+#pragma unroll
+        for (int p = 0; p < KP; ++p) av[p] = zaxpy(P.dt_62, k[r][p], av[p]);
+        st_chunk<Z, KP>(P.acc + base + r * K, av);
+      }
+    } else {
+      const int64_t ps = P.ring ? ring_slot(P.dir, i, P.Nt, P.R, P.Nstore) : -1;
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        Z av[KP];
+        ld_chunk<Z, KP>(P.acc + base + r * K, av);
+#pragma unroll
+        for (int p = 0; p < KP; ++p) av[p] = zaxpy(P.dt_6, k[r][p], av[p]);
+        st_chunk<Z, KP>(P.y + base + r * K, av);
+        if (ps >= 0 && RSVDT_CHECK_INDEX(ps < P.Nstore, 2))
+          st_chunk<Z, KP>(P.ring + ps * P.N * K + base + r * K, av);
+      }
+      if (br == 0 && q == 0) P.step[0] = i + 1;
+    }
+    return;
+  }
   if (S == 1) {
     if (P.Fh) {
       int64_t j2, j3;
@@ -825,7 +936,120 @@ static StepArgs<Z> make_args(rsvdt_ctx *ctx, int dir, bool forced) {
   P.dt_62 = (Rl)(dt / 6 * 2);
   P.step = ctx->d_step;
   P.rend = INT64_MAX;
+  P.fblk = nullptr;
   return P;
+}
+
+// ------------------------------------------- forcing block (complex64)
+//
+// The forcing synthesis (SourceCode/CreateForcingOnFly.c:17-19) for a block
+// of nblk <= kFbMaxSteps steps at once: every slab value is read once per
+// block instead of once per step, and the 2*nblk half-step forcings are
+// written to P.fblk (slot 2s: F2 of the block's step s, slot 2s+1: its F3).
+// A matrix product (2 nblk phasor rows) x (Nw slabs) x (N k values), FP32
+// FMA with the same operations in the same order as stage 1's own
+// synthesis (bit-identical forcings). One thread per (row, test vector)
+// holds that value's Nw slab coefficients in registers; the block's phasor
+// weights sit in shared memory, one row per half step: for pair slabs
+// [Re e_0, Im e_0, Re e_1 .. Re e_{H-1}, Im e_1 .. Im e_{H-1}, Re e_H,
+// Im e_H] (slab s >= 1 takes weight s + 1), for plain slabs the Nw complex
+// phasors. The block's first step and length go to step[2] and step[3].
+
+static const int kFbThreads = 256;
+static const int kFbMaxSteps = 16;  // largest forcing block (steps)
+
+template <int NW, bool PAIR>
+__global__ void __launch_bounds__(kFbThreads) k_forcing_block(const StepArgs<z64> P, int nblk) {
+  pdl_wait_and_release();
+  constexpr int ROW = ((PAIR ? NW + 2 : 2 * NW) + 3) / 4 * 4;
+  __shared__ __align__(16) float wt[2 * kFbMaxSteps][ROW];
+  const int64_t i_s = P.step[0];
+  for (int idx = threadIdx.x; idx < 2 * nblk * NW; idx += blockDim.x) {
+    const int m = idx / NW, s = idx - m * NW;
+    int64_t j2, j3;
+    step_idx(P.dir, i_s + m / 2, P.two_ns, j2, j3);
+    const z64 e = P.tab[((m & 1) ? j3 : j2) * NW + s];
+    if (PAIR) {
+      constexpr int H = NW / 2;
+      if (s == 0) {
+        wt[m][0] = e.re;
+        wt[m][1] = e.im;
+      } else if (s < H) {
+        wt[m][s + 1] = e.re;
+        wt[m][H + s] = e.im;
+      } else if (s == H) {
+        wt[m][NW] = e.re;
+        wt[m][NW + 1] = e.im;
+      }
+    } else {
+      wt[m][2 * s] = e.re;
+      wt[m][2 * s + 1] = e.im;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.step[2] = i_s;
+    P.step[3] = nblk;
+  }
+  __syncthreads();
+  const int64_t NK = P.N * P.K;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < NK; t += (int64_t)gridDim.x * blockDim.x) {
+    z64 v[NW];
+#pragma unroll
+    for (int s = 0; s < NW; ++s) {
+      const float2 u = __ldg(reinterpret_cast<const float2 *>(P.Fh + (int64_t)s * NK + t));
+      v[s] = zmake<z64>(u.x, u.y);
+    }
+    for (int m = 0; m < 2 * nblk; ++m) {
+      const float *w = wt[m];
+      z64 f = zmake<z64>(0, 0);
+      if (PAIR) {
+        zmac(f, v[0], zmake<z64>(w[0], w[1]));
+#pragma unroll
+        for (int s = 1; s <= NW - 2; ++s) {
+          f.re = fmaf(w[s + 1], v[s].re, f.re);
+          f.im = fmaf(w[s + 1], v[s].im, f.im);
+        }
+        zmac(f, v[NW - 1], zmake<z64>(w[NW], w[NW + 1]));
+      } else {
+#pragma unroll
+        for (int s = 0; s < NW; ++s) zmac(f, v[s], zmake<z64>(w[2 * s], w[2 * s + 1]));
+      }
+      *reinterpret_cast<float2 *>(P.fblk + (int64_t)m * NK + t) = make_float2(f.re, f.im);
+    }
+  }
+}
+
+// Whether a forcing block can serve these stage arguments: complex64 5x5
+// block-row stages (k_bstage) with the forcing on and Nw in 8..64 (powers
+// of two, the slab counts compiled into k_forcing_block).
+static bool forcing_block_applies(const StepArgs<z64> &P) {
+  if (!P.Fh || P.bs != 5) return false;
+  switch (P.K) {
+    case 2: case 4: case 6: case 8: case 10: case 16: break;
+    default: return false;
+  }
+  return P.Nw == 8 || P.Nw == 16 || P.Nw == 32 || P.Nw == 64;
+}
+
+template <int NW>
+static void launch_forcing_block_nw(const StepArgs<z64> &P, int nblk, int grid, cudaStream_t st) {
+  if (P.pair)
+    launch_pdl(k_forcing_block<NW, true>, grid, kFbThreads, 0, st, P, nblk);
+  else
+    launch_pdl(k_forcing_block<NW, false>, grid, kFbThreads, 0, st, P, nblk);
+}
+
+// The forcing of the next nblk steps (from the device step counter) into
+// P.fblk; grid: a few blocks per SM, each striding over the values.
+static void launch_forcing_block(const StepArgs<z64> &P, int nblk, int sm_count, cudaStream_t st) {
+  const int64_t NK = P.N * P.K;
+  const int grid = (int)std::min<int64_t>((NK + kFbThreads - 1) / kFbThreads, (int64_t)4 * std::max(sm_count, 1));
+  switch (P.Nw) {
+    case 8: launch_forcing_block_nw<8>(P, nblk, grid, st); break;
+    case 16: launch_forcing_block_nw<16>(P, nblk, grid, st); break;
+    case 32: launch_forcing_block_nw<32>(P, nblk, grid, st); break;
+    default: launch_forcing_block_nw<64>(P, nblk, grid, st); break;
+  }
 }
 
 // ---------------------------------------------------------- dispatch
@@ -847,6 +1071,17 @@ static void launch_bstage(int stage, const StepArgs<Z> &P, cudaStream_t st) {
       default: launch_pdl(k_rstage<Z, K, 4>, gr, kRowThreads, 0, st, P); break;
     }
     return;
+  }
+  if constexpr (sizeof(Z) == 8) {
+    if (P.fblk) {
+      switch (stage) {
+        case 1: launch_pdl(k_bstage<Z, K, KP, 1, true>, g, kRowThreads, 0, st, P); break;
+        case 2: launch_pdl(k_bstage<Z, K, KP, 2, true>, g, kRowThreads, 0, st, P); break;
+        case 3: launch_pdl(k_bstage<Z, K, KP, 3, true>, g, kRowThreads, 0, st, P); break;
+        default: launch_pdl(k_bstage<Z, K, KP, 4, true>, g, kRowThreads, 0, st, P); break;
+      }
+      return;
+    }
   }
   switch (stage) {
     case 1: launch_pdl(k_bstage<Z, K, KP, 1>, g, kRowThreads, sm, st, P); break;
@@ -919,38 +1154,115 @@ rsvdt_status launch_forcing_init(rsvdt_ctx *ctx, int dir, int prec) {
 }
 
 static const int64_t kGraphSteps = 16;
+// Device memory a forcing block leaves free for everything else (dense-stage
+// scratch, transfers) when it is allocated.
+static const size_t kFbHeadroom = (size_t)4 << 30;
+
+static void free_step_graphs(rsvdt_ctx *ctx) {
+  for (auto &g : ctx->step_graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+// Turns on the forcing block for these stage arguments when it applies and
+// its buffer (2 G N k complex64 values) fits with kFbHeadroom to spare;
+// *G = the block length, 0 when stage 1 synthesises the forcing (which is
+// not an error: the stage kernels then synthesise it themselves).
+static void prepare_forcing_block(rsvdt_ctx *ctx, StepArgs<z64> &P, int *G) {
+  *G = 0;
+  if (ctx->fb_steps == 0 || !forcing_block_applies(P)) return;
+  const int g = ctx->fb_steps < 0 ? kFbMaxSteps : ctx->fb_steps;
+  const size_t need = sizeof(z64) * 2 * (size_t)g * (size_t)P.N * (size_t)P.K;
+  if (ctx->fb_bytes < need) {
+    dfree(ctx, ctx->fblk);
+    ctx->fblk = nullptr;
+    ctx->fb_bytes = 0;
+    free_step_graphs(ctx);  // captured with the old buffer
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    if (fr < need + kFbHeadroom) return;
+    ctx->fblk = dalloc(ctx, need);
+    if (!ctx->fblk) return;
+    ctx->fb_bytes = need;
+  }
+  if (!ctx->sm_count) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess) {
+      cudaGetLastError();
+      n = 1;
+    }
+    ctx->sm_count = n;
+  }
+  P.fblk = (z64 *)ctx->fblk;
+  *G = g;
+}
+
+// n steps as stage launches, preceded (G > 0) by one forcing-block launch
+// per block of at most G steps; returns the kernels launched.
+template <class Z>
+static int64_t enqueue_steps(rsvdt_ctx *ctx, const StepArgs<Z> &P, int64_t n, int G) {
+  if (G <= 0) {
+    for (int64_t s = 0; s < n; ++s) enqueue_step(ctx, P);
+    return 4 * n;
+  }
+  int64_t launches = 0;
+  if constexpr (sizeof(Z) == 8) {
+    for (int64_t done = 0; done < n;) {
+      const int nb = (int)std::min<int64_t>(G, n - done);
+      launch_forcing_block(P, nb, ctx->sm_count, ctx->stream);
+      for (int s = 0; s < nb; ++s) enqueue_step(ctx, P);
+      launches += 1 + 4 * nb;
+      done += nb;
+    }
+  }
+  return launches;
+}
 
 template <class Z>
 static rsvdt_status run_steps_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t nsteps) {
   auto P = make_args<Z>(ctx, dir, true);
+  int G = 0;
+  if constexpr (sizeof(Z) == 8) {
+    prepare_forcing_block(ctx, P, &G);
+    ctx->fb_last = G;
+  }
   k_set_step<<<1, 1, 0, ctx->stream>>>(ctx->d_step, i0);
   ctx->launches += 1;
   int64_t full = nsteps / kGraphSteps, rest = nsteps % kGraphSteps;
   if (full > 0) {
     cudaGraphExec_t &ge = ctx->step_graph[dir ? 1 : 0];
     int &gprec = ctx->step_graph_prec[dir ? 1 : 0];
+    int &gfb = ctx->step_graph_fb[dir ? 1 : 0];
     const int prec = sizeof(Z) == sizeof(z64) ? RSVDT_PREC_C64 : RSVDT_PREC_C128;
-    if (ge && gprec != prec) {
+    if (ge && (gprec != prec || gfb != G)) {
       cudaGraphExecDestroy(ge);
       ge = nullptr;
     }
+    int64_t per_graph = 0;
     if (!ge) {
       gprec = prec;
+      gfb = G;
       cudaGraph_t g;
       if (!cuda_ok(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal),
                    "begin capture"))
         return RSVDT_ERR_CUDA;
-      for (int64_t s = 0; s < kGraphSteps; ++s) enqueue_step(ctx, P);
+      per_graph = enqueue_steps(ctx, P, kGraphSteps, G);
       if (!cuda_ok(ctx, cudaStreamEndCapture(ctx->stream, &g), "end capture")) return RSVDT_ERR_CUDA;
       if (!cuda_ok(ctx, cudaGraphInstantiate(&ge, g, 0), "graph instantiate")) return RSVDT_ERR_CUDA;
       cudaGraphDestroy(g);
+    } else {
+      per_graph = 4 * kGraphSteps + (G > 0 ? (kGraphSteps + G - 1) / G : 0);
     }
     for (int64_t c = 0; c < full; ++c)
       if (!cuda_ok(ctx, cudaGraphLaunch(ge, ctx->stream), "graph launch")) return RSVDT_ERR_CUDA;
-    ctx->launches += full * kGraphSteps * 4;
+    ctx->launches += full * per_graph;
   }
-  for (int64_t s = 0; s < rest; ++s) enqueue_step(ctx, P);
-  ctx->launches += rest * 4;
+  ctx->launches += enqueue_steps(ctx, P, rest, G);
   if (!cuda_ok(ctx, cudaGetLastError(), "rk4 steps")) return RSVDT_ERR_CUDA;
   return RSVDT_OK;
 }
@@ -1204,7 +1516,18 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_steps(const Step
 // engine does not apply).
 template <class Z>
 static int cluster_shape(int64_t NK, int *threads) {
-  static int max_cluster = -1;
+  // Largest launchable cluster per device ordinal (devices may differ in
+  // SM count or partitioning), stored plus one so that the zero-initialised
+  // 0 means "not yet queried". Concurrent first queries from several host
+  // threads compute and store the same value.
+  constexpr int kMaxDevices = 64;
+  static std::atomic<int> max_cluster_dev[kMaxDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return 0;
+  }
+  int max_cluster = max_cluster_dev[dev].load(std::memory_order_acquire) - 1;
   if (max_cluster < 0) {
     max_cluster = 0;
     if (cudaFuncSetAttribute(k_cluster_steps<Z>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
@@ -1223,6 +1546,7 @@ static int cluster_shape(int64_t NK, int *threads) {
     }
     cudaGetLastError();
     if (max_cluster > 16) max_cluster = 16;
+    max_cluster_dev[dev].store(max_cluster + 1, std::memory_order_release);
   }
   // As many SMs as a cluster can have (the stages' FP64 work spreads over
   // them), one thread per value.
@@ -1361,14 +1685,35 @@ template <class Z>
 static rsvdt_status profile_steps_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t nsteps,
                                     double *stage_ms) {
   auto P = make_args<Z>(ctx, dir, true);
-  cudaEvent_t ev[5];
+  int G = 0;
+  if constexpr (sizeof(Z) == 8) prepare_forcing_block(ctx, P, &G);
+  cudaEvent_t ev[5], fb0 = nullptr, fb1 = nullptr;
   for (auto &e : ev)
     if (!cuda_ok(ctx, cudaEventCreate(&e), "event create")) return RSVDT_ERR_CUDA;
+  if (G > 0 && (!cuda_ok(ctx, cudaEventCreate(&fb0), "event create") ||
+                !cuda_ok(ctx, cudaEventCreate(&fb1), "event create")))
+    return RSVDT_ERR_CUDA;
   k_set_step<<<1, 1, 0, ctx->stream>>>(ctx->d_step, i0);
   ctx->launches += 1;
-  for (int s = 0; s < 4; ++s) stage_ms[s] = 0;
+  for (int s = 0; s < 5; ++s) stage_ms[s] = 0;
   rsvdt_status st = RSVDT_OK;
   for (int64_t n = 0; n < nsteps && st == RSVDT_OK; ++n) {
+    if constexpr (sizeof(Z) == 8) {
+      if (G > 0 && n % G == 0) {
+        // The next block's forcing, timed on its own.
+        cudaEventRecord(fb0, ctx->stream);
+        launch_forcing_block(P, (int)std::min<int64_t>(G, nsteps - n), ctx->sm_count, ctx->stream);
+        cudaEventRecord(fb1, ctx->stream);
+        ctx->launches += 1;
+        if (!cuda_ok(ctx, cudaEventSynchronize(fb1), "event sync")) {
+          st = RSVDT_ERR_CUDA;
+          break;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, fb0, fb1);
+        stage_ms[4] += ms;
+      }
+    }
     cudaEventRecord(ev[0], ctx->stream);
     for (int s = 1; s <= 4; ++s) {
       launch_stage(s, P, ctx->stream);
@@ -1386,6 +1731,8 @@ static rsvdt_status profile_steps_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t
     }
   }
   for (auto &e : ev) cudaEventDestroy(e);
+  if (fb0) cudaEventDestroy(fb0);
+  if (fb1) cudaEventDestroy(fb1);
   if (st == RSVDT_OK && !cuda_ok(ctx, cudaGetLastError(), "profile steps")) st = RSVDT_ERR_CUDA;
   return st;
 }

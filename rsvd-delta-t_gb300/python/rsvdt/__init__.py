@@ -39,7 +39,8 @@ EXPORTED = [
     "rsvdt_qr_all_freqs", "rsvdt_svd_all_freqs", "rsvdt_power_iteration", "rsvdt_set_checkpoint", "rsvdt_run",
     "rsvdt_debug_build",
     "rsvdt_get_results", "rsvdt_rk4_steps", "rsvdt_rk4_reset", "rsvdt_rk4_advance",
-    "rsvdt_rk4_profile", "rsvdt_synchronize", "rsvdt_stream", "rsvdt_launch_count",
+    "rsvdt_rk4_profile", "rsvdt_rk4_profile_ex", "rsvdt_set_forcing_block", "rsvdt_get_forcing_block",
+    "rsvdt_synchronize", "rsvdt_stream", "rsvdt_launch_count",
     "rsvdt_qr_all_freqs_noalloc", "rsvdt_trans_grid", "rsvdt_trans_run",
     "rsvdt_set_capacity_mode", "rsvdt_get_capacity", "rsvdt_get_result_cols", "rsvdt_device_memory",
     "rsvdt_set_lanes_per_row", "rsvdt_get_lanes_per_row", "rsvdt_get_timings", "rsvdt_reset_timings",
@@ -54,11 +55,14 @@ EXPORTED = [
 ]
 
 
-def qr_all_freqs_noalloc(Y_dev: int, Q_dev: int, rows: int, nw: int, k: int, stream: int = 0) -> None:
+def qr_all_freqs_noalloc(Y_dev: int, Q_dev: int, rows: int, nw: int, k: int, stream) -> None:
     """Binding of rsvdt_qr_all_freqs_noalloc: orthonormalises each
     frequency block of a caller-allocated device array (device pointers as
     integers, layout [row][iw][k] complex128) without allocating any device
-    memory. Raises RsvdtError with the library's message on failure."""
+    memory. `stream` is a cudaStream_t as an integer (e.g. a torch stream's
+    `cuda_stream`), or None / 0 for the legacy default stream, which
+    synchronises with every blocking stream and so breaks a capture open on
+    one of them. Raises RsvdtError with the library's message on failure."""
     lib = load_library()
     buf = C.create_string_buffer(512)
     st = lib.rsvdt_qr_all_freqs_noalloc(C.c_void_p(Y_dev), C.c_void_p(Q_dev), rows, nw, k,
@@ -153,6 +157,9 @@ def load_library(path: str | None = None) -> C.CDLL:
         "rsvdt_rk4_reset": (C.c_int, [vp, C.c_int]),
         "rsvdt_rk4_advance": (C.c_int, [vp, C.c_int, i64, i64]),
         "rsvdt_rk4_profile": (C.c_int, [vp, C.c_int, i64, i64, d]),
+        "rsvdt_rk4_profile_ex": (C.c_int, [vp, C.c_int, i64, i64, d]),
+        "rsvdt_set_forcing_block": (C.c_int, [vp, C.c_int32]),
+        "rsvdt_get_forcing_block": (C.c_int32, [vp]),
         "rsvdt_qr_all_freqs_noalloc": (C.c_int, [vp, vp, i64, i64, i64, vp, C.c_char_p, i64]),
         "rsvdt_set_capacity_mode": (C.c_int, [vp, i64, C.c_int32]),
         "rsvdt_get_capacity": (C.c_int, [vp, P(i64)]),
@@ -391,6 +398,22 @@ class Context:
         self._check(self._lib.rsvdt_rk4_profile(self._h, direction, i0, nsteps,
                                                 out.ctypes.data_as(C.POINTER(C.c_double))))
         return out.tolist()
+
+    def rk4_profile_ex(self, direction: int, i0: int, nsteps: int) -> list:
+        """[stage 1, 2, 3, 4, forcing block] device time (ms, summed over
+        nsteps) from CUDA events (rsvdt_rk4_profile_ex)."""
+        out = np.zeros(5)
+        self._check(self._lib.rsvdt_rk4_profile_ex(self._h, direction, i0, nsteps,
+                                                   out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out.tolist()
+
+    def set_forcing_block(self, steps: int) -> None:
+        """Forcing synthesised ahead in blocks of `steps` steps (complex64
+        block-row stages; 0 = in stage 1, -1 = automatic)."""
+        self._check(self._lib.rsvdt_set_forcing_block(self._h, steps))
+
+    def forcing_block(self) -> int:
+        return int(self._lib.rsvdt_get_forcing_block(self._h))
 
     def timings(self) -> dict:
         """Wall time per phase (rsvdt_get_timings) as a dict."""

@@ -11,9 +11,10 @@ Writes, next to this script:
                            gains for the full tutorial run (k=10, q=1,
                            transient removal) on a seeded sketch.
 
-Run from the repository root: python tests/golden/make_golden.py
-It reads the reference checkout given by RSVDT_REFERENCE (default
-/root/reference); the fixtures it writes are what the tests read.
+Run from the repository root:
+    python tests/golden/make_golden.py <reference checkout>
+(or set RSVDT_REFERENCE to the checkout); the fixtures it writes are what
+the tests read.
 """
 import json
 import os
@@ -31,7 +32,6 @@ sys.path.insert(0, os.path.join(ROOT, "rsvd-delta-t_gb300", "python"))
 import oracle  # noqa: E402
 from rsvdt import petsc_io, synth  # noqa: E402
 
-REF = os.environ.get("RSVDT_REFERENCE", "/root/reference")
 
 # variables.yaml:16-39 (k, q, Nw, w, TwoPI, TransientLength, dt,
 # TransientRemoval, RandSeed).
@@ -39,8 +39,16 @@ TUTORIAL = dict(k=10, q=1, Nw=42, w=0.05, TwoPI=False, TransientLength=10.0, dt=
                 TransientRemoval=True, RandSeed=14)
 
 
+def reference_root():
+    """The reference checkout: the first argument, else RSVDT_REFERENCE."""
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RSVDT_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference checkout> (or set RSVDT_REFERENCE)")
+    return ref
+
+
 def main():
-    src = os.path.join(REF, "Tutorial", "Ginzburg-Landau", "A_GL")
+    src = os.path.join(reference_root(), "Tutorial", "Ginzburg-Landau", "A_GL")
     dst = os.path.join(HERE, "A_GL")
     shutil.copyfile(src, dst)
     A = petsc_io.read_mat(dst)
