@@ -242,6 +242,148 @@ def parity_batch(fam, sketches, params, S_batched: dict, threads: int, q: int, c
     return out
 
 
+TTG_TOL = 1e-3  # relative gain error that time-to-gains is measured at
+
+
+def gain_rel_err(S, S_exact, jmax: int = 3) -> float:
+    """max over frequencies and j <= jmax of |s_j - sigma_j| / sigma_j,
+    sigma_j the exact resolvent gains (k x Nw, as the results' S)."""
+    j = min(jmax, S.shape[0], S_exact.shape[0])
+    return float((np.abs(S[:j] - S_exact[:j]) / S_exact[:j]).max())
+
+
+def ttg_search(run, S_exact, plans, q_max: int, log=None):
+    """Time to gains of one solver form: for each plan (transient periods,
+    transient removal, dt factor), q = 0, 1, ... until the gains are within
+    TTG_TOL of the exact ones (max over j <= 3 and all frequencies); a run
+    already slower than the best time found ends its plan (a larger q costs
+    more). run(q, periods, tr, dtf) -> (seconds, S). Returns (best, trace):
+    best = the fastest run that met the tolerance (None if none did)."""
+    best, trace = None, []
+    for periods, tr, dtf in plans:
+        for q in range(q_max + 1):
+            t, S = run(q, periods, tr, dtf)
+            e = gain_rel_err(S, S_exact)
+            e1 = gain_rel_err(S, S_exact, 1)
+            rec = {"q": q, "periods": periods, "tr": int(tr), "dt_factor": dtf, "s": round(t, 4),
+                   "err_j<=3": float(f"{e:.3e}"), "err_j1": float(f"{e1:.3e}")}
+            trace.append(rec)
+            if log:
+                log(rec)
+            if e <= TTG_TOL:
+                if best is None or t < best["s"]:
+                    best = rec
+                break
+            if best is not None and t >= best["s"]:
+                break
+    return best, trace
+
+
+def ttg_gl1(q_max: int = 8):
+    """Time to gains on the 500-node Ginzburg-Landau configuration (k = 10,
+    64 frequencies j*0.1, j = -32..31, dt = T/4096) against the dense FP64
+    resolvent: plain complex128 against the precision forms."""
+    import oracle
+    import rsvdt
+    from rsvdt import synth, workloads
+
+    wl = workloads.make_gl1(k=10)
+    F = synth.gl_sketch(500, 10, 64)
+    om = [oracle.freq_of(i, 64, 0.1) for i in range(64)]
+    Sx = oracle.dense_resolvent_svd(wl.csr, om, 3)[0]
+    T = 2 * np.pi / 0.1
+
+    def runner(prec):
+        def run(q, periods, tr, dtf):
+            p = rsvdt.default_params(k=10, q=q, Nw=64, w=0.1, dt=wl.dt_in * dtf, TransientLength=periods * T,
+                                     TransientRemoval=int(tr), precision=prec, Display=0)
+            ctx = rsvdt.Context(p)
+            ctx.set_operator(wl.csr)
+            ctx.set_sketch(F)
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            ctx.run()
+            S = ctx.get_results(U=False, V=False)[2]
+            t = time.perf_counter() - t0
+            ctx.close()
+            return t, S
+        return run
+
+    plans = [(1, 0, 1.0), (2, 0, 1.0), (3, 0, 1.0), (1, 1, 1.0)]
+    return ttg_forms(runner, Sx, plans, q_max,
+                     "GL1: N=500 Ginzburg-Landau, k=10, Nw=64, dt=T/4096; exact gains: dense FP64 SVD of "
+                     "(i w I - A)^-1")
+
+
+def ttg_3d24(q_max: int = 10, seed: int = 99):
+    """Time to gains on the five-field 3D operator at 24^3 (N = 69,120, the
+    3D64 configuration's k = 10, 32 frequencies, diagonal W, recorded
+    spectral shift, dt at the RK4 stability limit) against the exact
+    resolvent gains of tests/golden/exact_gains_op3d24.npz (sparse LU +
+    Lanczos, FP64)."""
+    import rsvdt
+    from rsvdt import workloads
+
+    fx = np.load(os.path.join(ROOT, "tests", "golden", "exact_gains_op3d24.npz"))
+    wl = workloads.make_3d(n=24, k=10, Nw=32)
+    assert "recorded" in wl.meta["shift_method"] and abs(float(fx["shift"]) - wl.meta["shift"]) < 1e-15
+    Sx = fx["S"]
+    T = 2 * np.pi / wl.w
+
+    def runner(prec):
+        def run(q, periods, tr, dtf):
+            p = rsvdt.default_params(k=wl.k, q=q, Nw=wl.Nw, w=wl.w, dt=wl.dt_in * dtf, TransientLength=periods * T,
+                                     TransientRemoval=int(tr), precision=prec, Display=0)
+            ctx = rsvdt.Context(p)
+            ctx.set_operator_bcsr(*wl.bcsr)
+            ctx.set_weight(rsvdt.W_Q_SQRT, wl.weights["W_sqrt"])
+            ctx.set_weight(rsvdt.W_F_SQRT_INV, wl.weights["W_sqrt_inv"])
+            ctx.set_weight(rsvdt.W_Q_SQRT_INV, wl.weights["W_sqrt_inv"])
+            ctx.random_sketch(seed)
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            ctx.run()
+            S = ctx.get_results(U=False, V=False)[2]
+            t = time.perf_counter() - t0
+            ctx.close()
+            return t, S
+        return run
+
+    plans = [(2, 0, 1.0), (3, 0, 1.0), (2, 1, 1.0), (3, 0, 0.5)]
+    return ttg_forms(runner, Sx, plans, q_max,
+                     f"3D24: N={wl.N} five-field operator (5x5 blocks), k=10, Nw=32, diagonal W, shift "
+                     f"{wl.meta['shift']:.6g} ({wl.meta['shift_method']}), dt={wl.dt_in:.4g} (RK4 limit); exact "
+                     "gains: sparse LU + Lanczos (tests/golden/exact_gains_op3d24.npz)")
+
+
+def ttg_forms(runner, Sx, plans, q_max, workload):
+    """ttg_search for the plain form and the two precision forms; each form
+    is run once untimed first (kernel loading)."""
+    import rsvdt
+
+    out = {"workload": workload, "tolerance": TTG_TOL,
+           "search": "per plan (transient periods, transient removal, dt factor): q = 0, 1, ... until "
+                     "max_{w, j<=3} |s_j - sigma_j| / sigma_j <= 1e-3; fastest such run",
+           "plans": [list(pl) for pl in plans], "sigma1_range": [float(Sx[0].min()), float(Sx[0].max())]}
+    for name, prec in (("plain_c128", rsvdt.PREC_C128), ("precision_c64", rsvdt.PREC_C64),
+                       ("precision_c64_refine", rsvdt.PREC_C64_REFINE)):
+        run = runner(prec)
+        run(0, plans[0][0], plans[0][1], plans[0][2])  # warm-up
+        best, trace = ttg_search(run, Sx, plans, q_max,
+                                 log=lambda r, n=name: print(f"ttg {n} {r}", file=sys.stderr, flush=True))
+        out[name] = {"best": best, "trace": trace}
+    base = out["plain_c128"]["best"]
+    chosen = [(out[n]["best"]["s"], n) for n in ("precision_c64", "precision_c64_refine") if out[n]["best"]]
+    if base and chosen:
+        t, n = min(chosen)
+        out["chosen"] = n
+        out["ratio_plain_over_chosen"] = round(base["s"] / t, 3)
+    else:
+        out["chosen"] = None
+        out["ratio_plain_over_chosen"] = None
+    return out
+
+
 def time_to_gains(n: int, seed: int = 4321):
     """Full RSVD-Delta-t solve (SourceCode/main.c:134-144: direct action,
     q = 1 power iteration, SVDs, adjoint action) on the 3D operator of an
