@@ -319,7 +319,7 @@ def ttg_gl1(q_max: int = 8):
                      "(i w I - A)^-1")
 
 
-def ttg_3d24(q_max: int = 8, seed: int = 99):
+def ttg_3d24(q_max: int = 24, seed: int = 99):
     """Time to gains on the five-field 3D operator at 24^3 (N = 69,120, the
     3D64 configuration's k = 10, 32 frequencies, diagonal W, recorded
     spectral shift, dt at the RK4 stability limit) against the exact
@@ -353,9 +353,13 @@ def ttg_3d24(q_max: int = 8, seed: int = 99):
             return t, S
         return run
 
-    plans = [(2, 0, 1.0), (3, 0, 1.0), (2, 1, 1.0)]
+    # The transient decays as exp(-0.05 t) (rightmost eigenvalue -0.05): two
+    # periods leave 2e-3 of it, three 8e-5. Transient removal is not in the
+    # plans: its FP64 Galerkin step costs more per action here than a third
+    # period does.
+    plans = [(2, 0, 1.0), (3, 0, 1.0)]
     return ttg_forms(runner, lambda S, j: gain_rel_err(S, Sx, j), [float(Sx[0].min()), float(Sx[0].max())],
-                     plans, q_max,
+                     plans, q_max, budget_s=240.0, workload=
                      f"3D24: N={wl.N} five-field operator (5x5 blocks), k=10, Nw=32, diagonal W, shift "
                      f"{wl.meta['shift']:.6g} ({wl.meta['shift_method']}), dt={wl.dt_in:.4g} (RK4 limit); exact "
                      "gains: sparse LU + Lanczos (tests/golden/exact_gains_op3d24.npz)")
@@ -452,7 +456,7 @@ def ttg_forms(runner, err, sigma1_range, plans, q_max, workload, forms=None, bud
     return out
 
 
-def ttg_batch(q_max: int = 8, sigma_max: float = 1e3, seed: int = 2024, budget_s: float = 240.0):
+def ttg_batch(q_max: int = 16, sigma_max: float = 1e3, seed: int = 2024, budget_s: float = 240.0):
     """Time to gains on the batching family (48 Ginzburg-Landau problems, N
     log-uniform in [200, 20000], k in {6, 10, 16}, Nw in {16, 32, 64}, one
     transient period) against the exact resolvent gains of
@@ -845,16 +849,14 @@ def learned_form(n_train: int = 200, n_held: int = 20, N: int = 2000, seed: int 
     fam = learned.Family(N=N, k=10, Nw=16)
     train = fam.points(n_train, seed=seed)
     held = fam.points(n_held, seed=seed + 1)
-    # Exact gains of the held-out points (host cores; process pool started
-    # with spawn).
+    # Exact gains of the held-out points (host, one core: tridiagonal LU).
     t0 = time.perf_counter()
     Sx = []
     for pt in held:
         A, beta = fam.operator(pt)
         if beta > 0:
             A = (A - beta * sp.eye(A.shape[0], format="csr")).tocsr()
-        Sx.append(oracle.sparse_resolvent_svd(A, list(fam.omegas()), 3, tol=1e-12,
-                                              procs=min(8, os.cpu_count() or 1))[0])
+        Sx.append(oracle.sparse_resolvent_svd(A, list(fam.omegas()), 3, tol=1e-12)[0])
     t_exact = time.perf_counter() - t0
     res, t_data = learned.solve_batch(fam, train, q=1, precision=rsvdt.PREC_C64, seed=seed * 10)
     ls = learned.LearnedSketch(fam, r=64, hidden=256, depth=4, seed=1)
