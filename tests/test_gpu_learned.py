@@ -55,29 +55,41 @@ def test_training_fits_a_smooth_map(built_lib):
 def test_learned_sketch_beats_random_at_q0(built_lib):
     """Small Ginzburg-Landau family (N = 200): the network trained on the
     method's own forcing modes at 40 points gives, at held-out points with
-    no power iteration, smaller gain errors than the random sketch, measured
-    against a converged solve (q = 3)."""
+    no power iteration, smaller leading-gain errors than the random sketch,
+    measured against the exact resolvent gains (dense FP64 SVD of
+    (i w I - A)^-1). The FP64 gain check that decides the fallback is run on
+    the learned q = 0 results; the fallback count is printed."""
+    import scipy.sparse as sp
+
+    import oracle
     import rsvdt
     from rsvdt import learned
 
     fam = learned.Family(N=200, k=4, Nw=8)
     train = fam.points(40, seed=11)
     held = fam.points(8, seed=12)
-    res, _ = learned.solve_batch(fam, train, q=1, precision=rsvdt.PREC_C64, seed=100)
+    res, _ = learned.solve_batch(fam, train, q=2, precision=rsvdt.PREC_C64, seed=100)
     ls = learned.LearnedSketch(fam, r=16, hidden=64, depth=4, seed=1)
     ls.fit(train, [V for (_, V, _) in res], steps=2000, batch=64, lr=2e-3)
-    ref, _ = learned.solve_batch(fam, held, q=3, precision=rsvdt.PREC_C128, seed=500)
+    exact = []
+    for pt in held:
+        A, beta = fam.operator(pt)
+        A = (A - beta * sp.eye(A.shape[0], format="csr")).tocsr() if beta > 0 else A
+        exact.append(oracle.dense_resolvent_svd(A, list(fam.omegas()), 1)[0])
     rnd, _ = learned.solve_batch(fam, held, q=0, precision=rsvdt.PREC_C128, seed=600)
     lrn, _ = learned.solve_batch(fam, held, q=0, precision=rsvdt.PREC_C128,
                                  sketches=[ls.sketch(p) for p in held])
-    e_rnd, _ = learned.gain_errors(rnd, ref)
-    e_lrn, _ = learned.gain_errors(lrn, ref)
-    assert np.isfinite(e_lrn).all() and np.isfinite(e_rnd).all()
-    print("3D family 8^3: POD energy", ls.pod_energy, "median sigma_1 error learned q0", np.median(e_lrn),
-          "random q0", np.median(e_rnd))
-    # The FP64 gain check that decides the fallback runs and is finite.
-    chk = learned.gain_check(fam, held[0], lrn[0])
-    assert np.isfinite(chk)
+
+    def err(results):
+        return np.array([float((np.abs(S[0] - Sx[0]) / Sx[0]).max()) for (_, _, S), Sx in zip(results, exact)])
+
+    e_rnd, e_lrn = err(rnd), err(lrn)
+    checks = [learned.gain_check(fam, p, r, jmax=1) for p, r in zip(held, lrn)]
+    print("GL family N=200: POD energy", ls.pod_energy, "median sigma_1 error against the exact gains: learned q0",
+          np.median(e_lrn), "random q0", np.median(e_rnd), "; learned runs failing the FP64 gain check (fallbacks):",
+          sum(c > 1e-3 for c in checks), "of", len(checks))
+    assert np.isfinite(e_lrn).all() and np.isfinite(e_rnd).all() and np.isfinite(checks).all()
+    assert np.median(e_lrn) < np.median(e_rnd)
 
 
 def test_learned_sketch_3d_family_small(built_lib):
