@@ -768,7 +768,8 @@ def gl1_form(threads: int):
     return out
 
 
-def large_precision_form(n: int = 128, k: int = 16, Nw: int = 64, periods: float = 1.0, seed: int = 99):
+def large_precision_form(n: int = 128, k: int = 16, Nw: int = 64, periods: float = 1.0, seed: int = 99,
+                         full_c128: bool = False):
     """Precision form on the 3D operator at n^3 (n = 128: N = 10.5M, 14.6M
     5x5 blocks, k = 16, 64 frequencies, q = 1): variant 1 = complex64 stages
     with FP32 accumulation, FP64 DFT/QR/SVD and the FP64 sweep (the last
@@ -776,7 +777,9 @@ def large_precision_form(n: int = 128, k: int = 16, Nw: int = 64, periods: float
     spectral block is 172 GB, so both run in capacity mode (test vectors in
     chunks, U in host memory in complex64). Wall time of the whole sequence,
     per-stage times of one chunk step, and variant 1's gain and first-mode
-    (V) errors against variant 2. `periods` transient periods."""
+    (V) errors against variant 2. `periods` transient periods. Unless
+    full_c128, variant 2 is timed by its chunk stage times only (its whole
+    sequence takes about 24 minutes)."""
     import rsvdt
     from rsvdt import workloads
 
@@ -801,8 +804,21 @@ def large_precision_form(n: int = 128, k: int = 16, Nw: int = 64, periods: float
         # complex128 stage kernels as the variant uses them.
         ctx.rk4_reset(rsvdt.DIRECT)
         st = [x / 2 for x in ctx.rk4_profile(rsvdt.DIRECT, 1, 2)]
+        if prec == rsvdt.PREC_C128 and not full_c128:
+            out[name] = {"chunk_k": kc, "Ns": g.Ns, "Nt": g.Nt, "steps_per_action": g.Ns + g.Nt,
+                         "chunk_stage_ms": [round(x, 3) for x in st],
+                         "run_s_estimate": round(4 * (k // kc) * (g.Ns + g.Nt) * sum(st) / 1e3, 1)}
+            ctx.close()
+            continue
+        fb_note = None
+        if prec != rsvdt.PREC_C128:
+            ctx.rk4_reset(rsvdt.DIRECT)
+            t5 = [x / 2 for x in ctx.rk4_profile_ex(rsvdt.DIRECT, 1, 2)]
+            fb_note = {"forcing_block_steps": ctx.forcing_block(), "forcing_block_ms_per_step": round(t5[4], 3),
+                       "stage_ms_without_forcing": [round(x, 3) for x in t5[:4]]}
         ctx.random_sketch(seed)
         ctx.synchronize()
+        ctx.reset_timings()
         t1 = time.perf_counter()
         ctx.run()
         ctx.synchronize()
@@ -811,8 +827,15 @@ def large_precision_form(n: int = 128, k: int = 16, Nw: int = 64, periods: float
         _, V1 = ctx.get_result_cols([iw * k for iw in range(g.Nw_eff)], U=False, V=True)
         res[name] = (np.asfortranarray(S), V1)
         out[name] = {"run_s": round(run_s, 1), "chunk_k": kc, "Ns": g.Ns, "Nt": g.Nt,
-                     "steps_per_action": g.Ns + g.Nt, "chunk_stage_ms": [round(x, 3) for x in st]}
+                     "steps_per_action": g.Ns + g.Nt, "chunk_stage_ms": [round(x, 3) for x in st],
+                     "phase_s": {key: round(v, 2) for key, v in ctx.timings()["seconds"].items()}}
+        if fb_note:
+            out[name].update(fb_note)
         ctx.close()
+    out["sigma1_range_variant1"] = [float(res["variant1_c64_fp64_sweep"][0][0].min()),
+                                    float(res["variant1_c64_fp64_sweep"][0][0].max())]
+    if "variant2_plain_c128" not in res:
+        return out
     S1, V1 = res["variant1_c64_fp64_sweep"]
     S2, V2 = res["variant2_plain_c128"]
     rel = np.abs(S1 - S2) / S2
@@ -1099,6 +1122,7 @@ def main():
     ap.add_argument("--large-n", type=int, default=0,
                     help="run the precision form on the n^3 operator in capacity mode (128: the 10.5M-row case)")
     ap.add_argument("--large-periods", type=float, default=1.0, help="transient periods of the --large-n runs")
+    ap.add_argument("--large-full", action="store_true", help="run the whole complex128 sequence in --large-n too")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -1234,7 +1258,7 @@ def main():
         gl1 = gl1_form(min(os.cpu_count() or 1, 10))
     large = None
     if rank == 0 and args.large_n:
-        large = large_precision_form(n=args.large_n, periods=args.large_periods)
+        large = large_precision_form(n=args.large_n, periods=args.large_periods, full_c128=args.large_full)
 
     cpu = None
     if rank == 0 and not args.no_cpu:

@@ -231,8 +231,12 @@ rsvdt_status rsvdt_rk4_profile_ex(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int
  * steps = G (1, 2, 4, 8 or 16): one kernel forms the forcings of G steps at
  * once, reading the coefficients once per G steps, into a buffer of
  * 2 G N k complex64 values that stages 1-4 read (same operations in the same
- * order: identical results). -1 (default): 16 when the buffer fits with 4
- * GiB of device memory to spare, else 0. Other stage kernels ignore it. */
+ * order: identical results). The buffer is the half of the forcing-slab
+ * buffer that complex64 slabs leave unused (no extra memory) when G <=
+ * Nw_eff / 2; a longer block gets its own allocation if 4 GiB of device
+ * memory stay free, else the stage-1 synthesis runs. -1 (default): the
+ * largest of 16, 8, 4, 2, 1 that fits in the slab buffer's spare half.
+ * Other stage kernels ignore it. */
 rsvdt_status rsvdt_set_forcing_block(rsvdt_ctx *ctx, int32_t steps);
 /* Block length in use by the last complex64 stepping (0 = none). */
 int32_t rsvdt_get_forcing_block(const rsvdt_ctx *ctx);

@@ -318,9 +318,11 @@ static rsvdt_status ensure_buffers(rsvdt_ctx *ctx, int64_t K) {
     const size_t ce = cap_chunk_elems(ctx, Ks, rows);
     ctx->ring = dalloc(ctx, sizeof(z128) * ce);
     ctx->Fh = dalloc(ctx, sizeof(z128) * ce);
+    ctx->Fh_bytes = ctx->Fh ? sizeof(z128) * ce : 0;
   } else {
     ctx->ring = dalloc(ctx, sizeof(z128) * Nstore * N * K);
     ctx->Fh = dalloc(ctx, sizeof(z128) * N * Nwe * K);
+    ctx->Fh_bytes = ctx->Fh ? sizeof(z128) * N * Nwe * K : 0;
   }
   if (ctx->capacity) {
     // One working block, re-allocated only when it must grow (its contents

@@ -210,6 +210,8 @@ struct rsvdt_ctx {
   int fb_steps = -1;
   void *fblk = nullptr;
   size_t fb_bytes = 0;
+  void *fb_ptr = nullptr;  // the block buffer the cached graphs use
+  size_t Fh_bytes = 0;     // bytes allocated for the slabs (Fh)
   int step_graph_fb[2] = {-1, -1};
   int fb_last = 0;  // block length of the last complex64 stepping (0: none)
   int sm_count = 0;

@@ -1166,29 +1166,52 @@ static void free_step_graphs(rsvdt_ctx *ctx) {
     }
 }
 
-// Turns on the forcing block for these stage arguments when it applies and
-// its buffer (2 G N k complex64 values) fits with kFbHeadroom to spare;
-// *G = the block length, 0 when stage 1 synthesises the forcing (which is
-// not an error: the stage kernels then synthesise it themselves).
+// Turns on the forcing block for these stage arguments when it applies;
+// *G = the block length, 0 when stage 1 synthesises the forcing (not an
+// error: the stage kernels then synthesise it themselves). The buffer
+// (2 G N k complex64 values) is, where it fits, the unused half of the slab
+// buffer, which is sized for complex128 slabs while the complex64 slabs take
+// half of it (automatic G halved down to what fits there: Nw_eff / 2 steps);
+// otherwise its own allocation, made only with kFbHeadroom of device memory
+// to spare.
 static void prepare_forcing_block(rsvdt_ctx *ctx, StepArgs<z64> &P, int *G) {
   *G = 0;
   if (ctx->fb_steps == 0 || !forcing_block_applies(P)) return;
-  const int g = ctx->fb_steps < 0 ? kFbMaxSteps : ctx->fb_steps;
-  const size_t need = sizeof(z64) * 2 * (size_t)g * (size_t)P.N * (size_t)P.K;
-  if (ctx->fb_bytes < need) {
-    dfree(ctx, ctx->fblk);
-    ctx->fblk = nullptr;
-    ctx->fb_bytes = 0;
-    free_step_graphs(ctx);  // captured with the old buffer
-    size_t fr = 0, tot = 0;
-    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
-      cudaGetLastError();
-      return;
+  int g = ctx->fb_steps < 0 ? kFbMaxSteps : ctx->fb_steps;
+  const size_t per_step = sizeof(z64) * 2 * (size_t)P.N * (size_t)P.K;
+  const size_t slabs = sizeof(z64) * (size_t)P.Nw * (size_t)P.N * (size_t)P.K;
+  void *buf = nullptr;
+  if (ctx->Fh && ctx->Fh_bytes >= slabs) {
+    const size_t fit = (ctx->Fh_bytes - slabs) / per_step;
+    int gi = g;
+    if (ctx->fb_steps < 0)
+      while (gi > 1 && (size_t)gi > fit) gi /= 2;
+    if ((size_t)gi <= fit) {
+      buf = (unsigned char *)ctx->Fh + slabs;  // slabs is a multiple of 16 bytes (Nw_eff even)
+      g = gi;
     }
-    if (fr < need + kFbHeadroom) return;
-    ctx->fblk = dalloc(ctx, need);
-    if (!ctx->fblk) return;
-    ctx->fb_bytes = need;
+  }
+  if (!buf) {
+    const size_t need = per_step * (size_t)g;
+    if (ctx->fb_bytes < need) {
+      dfree(ctx, ctx->fblk);
+      ctx->fblk = nullptr;
+      ctx->fb_bytes = 0;
+      size_t fr = 0, tot = 0;
+      if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+      }
+      if (fr < need + kFbHeadroom) return;
+      ctx->fblk = dalloc(ctx, need);
+      if (!ctx->fblk) return;
+      ctx->fb_bytes = need;
+    }
+    buf = ctx->fblk;
+  }
+  if (buf != ctx->fb_ptr) {
+    free_step_graphs(ctx);  // captured with another buffer
+    ctx->fb_ptr = buf;
   }
   if (!ctx->sm_count) {
     int n = 0;
@@ -1198,7 +1221,7 @@ static void prepare_forcing_block(rsvdt_ctx *ctx, StepArgs<z64> &P, int *G) {
     }
     ctx->sm_count = n;
   }
-  P.fblk = (z64 *)ctx->fblk;
+  P.fblk = (z64 *)buf;
   *G = g;
 }
 
@@ -1686,7 +1709,10 @@ static rsvdt_status profile_steps_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t
                                     double *stage_ms) {
   auto P = make_args<Z>(ctx, dir, true);
   int G = 0;
-  if constexpr (sizeof(Z) == 8) prepare_forcing_block(ctx, P, &G);
+  if constexpr (sizeof(Z) == 8) {
+    prepare_forcing_block(ctx, P, &G);
+    ctx->fb_last = G;
+  }
   cudaEvent_t ev[5], fb0 = nullptr, fb1 = nullptr;
   for (auto &e : ev)
     if (!cuda_ok(ctx, cudaEventCreate(&e), "event create")) return RSVDT_ERR_CUDA;

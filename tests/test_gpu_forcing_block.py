@@ -46,7 +46,9 @@ def test_forcing_block_actions_are_bit_identical(built_lib, k, Nw, real):
             out.append(ctx.get_block())
         res[fb] = (out, ctx.forcing_block())
         ctx.close()
-    assert res[0][1] == 0 and res[-1][1] == 16 and res[4][1] == 4
+    # Automatic length: what fits in the spare half of the slab buffer.
+    nwe = Nw // 2 if real else Nw
+    assert res[0][1] == 0 and res[-1][1] == min(16, nwe // 2) and res[4][1] == 4
     for fb in (-1, 4):
         for a, b in zip(res[fb][0], res[0][0]):
             assert np.array_equal(a, b), fb
