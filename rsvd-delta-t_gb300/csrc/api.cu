@@ -702,6 +702,8 @@ void rsvdt_destroy(rsvdt_ctx *ctx) {
   }
   if (ctx->io_event) cudaEventDestroy(ctx->io_event);
   if (ctx->up_event) cudaEventDestroy(ctx->up_event);
+  for (auto &e : ctx->slab_event)
+    if (e) cudaEventDestroy(e);
   delete ctx;
 }
 
@@ -1308,6 +1310,13 @@ rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t 
          !cuda_ok(ctx, cudaEventCreateWithFlags(&ctx->io_event, cudaEventDisableTiming), "event create") ||
          !cuda_ok(ctx, cudaEventCreateWithFlags(&ctx->up_event, cudaEventDisableTiming), "event create")))
       return RSVDT_ERR_CUDA;
+    // y is downloaded in row slabs, each as soon as its rows of the last
+    // stage 4 are final, while the next slab computes.
+    const int nslab = stage4_slab_count(ctx, d, prec, rsvdt_ctx::kIoSlabs);
+    for (int k = 0; k < nslab; ++k)
+      if (!ctx->slab_event[k] &&
+          !cuda_ok(ctx, cudaEventCreateWithFlags(&ctx->slab_event[k], cudaEventDisableTiming), "event create"))
+        return RSVDT_ERR_CUDA;
     // The first step's forcing needs no state: it is synthesised on the
     // context's stream while y and F3 upload on the second stream.
     RSVDT_TRY(launch_forcing_ahead(ctx, d, prec, i0));
@@ -1320,19 +1329,28 @@ rsvdt_status rsvdt_rk4_steps(rsvdt_ctx *ctx, rsvdt_dir dir, int64_t i0, int64_t 
     RSVDT_TRY(launch_colmajor_to_blk(ctx, sf, N, N, K, (z128 *)ctx->F3));
     // F3 is final after the last step's stage 1: its transpose and download
     // run on the second stream while stages 2-4 run.
-    RSVDT_TRY(launch_first_step_rest(ctx, d, prec, i0, nsteps == 1 ? ctx->io_event : nullptr));
-    if (nsteps >= 2) {
+    if (nsteps == 1) {
+      RSVDT_TRY(launch_first_step_rest(ctx, d, prec, i0, ctx->io_event, nslab, ctx->slab_event));
+    } else {
+      RSVDT_TRY(launch_first_step_rest(ctx, d, prec, i0, nullptr));
       RSVDT_TRY(run_steps(ctx, d, prec, i0 + 1, nsteps - 2, true));
-      RSVDT_TRY(run_last_step_split(ctx, d, prec, i0 + nsteps - 1, ctx->io_event));
+      RSVDT_TRY(run_last_step_split(ctx, d, prec, i0 + nsteps - 1, ctx->io_event, nslab, ctx->slab_event));
     }
     if (!cuda_ok(ctx, cudaStreamWaitEvent(ctx->io_stream, ctx->io_event, 0), "wait")) return RSVDT_ERR_CUDA;
     RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->F3, N, K, sf, N, ctx->io_stream));
     if (!cuda_ok(ctx, cudaMemcpyAsync(F3, sf, bytes, cudaMemcpyDeviceToHost, ctx->io_stream), "download"))
       return RSVDT_ERR_CUDA;
-    RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->y, N, K, sy, N));
-    if (!cuda_ok(ctx, cudaMemcpyAsync(y, sy, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download") ||
-        !cuda_ok(ctx, cudaStreamSynchronize(ctx->io_stream), "sync"))
-      return RSVDT_ERR_CUDA;
+    for (int k = 0; k < nslab; ++k) {
+      const int64_t r0 = N * k / nslab, r1 = N * (k + 1) / nslab;
+      if (!cuda_ok(ctx, cudaStreamWaitEvent(ctx->io_stream, ctx->slab_event[k], 0), "wait")) return RSVDT_ERR_CUDA;
+      RSVDT_TRY(launch_blk_to_colmajor(ctx, (const z128 *)ctx->y + r0 * K, r1 - r0, K, sy + r0, N, ctx->io_stream));
+      if (!cuda_ok(ctx,
+                   cudaMemcpy2DAsync((z128 *)y + r0, sizeof(z128) * N, sy + r0, sizeof(z128) * N,
+                                     sizeof(z128) * (r1 - r0), K, cudaMemcpyDeviceToHost, ctx->io_stream),
+                   "download"))
+        return RSVDT_ERR_CUDA;
+    }
+    if (!cuda_ok(ctx, cudaStreamSynchronize(ctx->io_stream), "sync")) return RSVDT_ERR_CUDA;
   } else {
     // Host (N x K column-major) -> device [n][k], both arrays in flight.
     if (!cuda_ok(ctx, cudaMemcpyAsync(sy, y, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload") ||

@@ -133,6 +133,9 @@ struct rsvdt_ctx {
   // the last step's stages 2-4 run (created on first use).
   cudaStream_t io_stream = nullptr;
   cudaEvent_t io_event = nullptr, up_event = nullptr;
+  // ... and one event per row slab of the last stage 4 (y downloaded by slab).
+  static constexpr int kIoSlabs = 4;
+  cudaEvent_t slab_event[kIoSlabs] = {nullptr, nullptr, nullptr, nullptr};
   int64_t launches = 0;
   std::string err;
 
@@ -287,9 +290,16 @@ rsvdt_status launch_unforced_steps(rsvdt_ctx *ctx, int dir, z128 *cols, int64_t 
                                    int64_t nsteps);
 int step_lanes(const rsvdt_ctx *ctx);
 bool use_cluster_engine(const rsvdt_ctx *ctx, int prec, int *C, int *threads);
-rsvdt_status run_last_step_split(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1);
+// The last step of rsvdt_rk4_steps with events for the host transfers: after
+// stage 1 (F3 final) and, with slab_done, after each of nslab row slabs of
+// stage 4 (those rows of y final); stage4_slab_count says how many slabs
+// the step's stage-4 kernel can take (1: slab_done[0] follows the whole).
+int stage4_slab_count(rsvdt_ctx *ctx, int dir, int prec, int want);
+rsvdt_status run_last_step_split(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1,
+                                 int nslab = 1, cudaEvent_t *slab_done = nullptr);
 rsvdt_status launch_forcing_ahead(rsvdt_ctx *ctx, int dir, int prec, int64_t i);
-rsvdt_status launch_first_step_rest(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1);
+rsvdt_status launch_first_step_rest(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1,
+                                    int nslab = 1, cudaEvent_t *slab_done = nullptr);
 rsvdt_status debug_index_status(rsvdt_ctx *ctx);
 rsvdt_status launch_trans_steps(rsvdt_ctx *ctx, double dt, z128 *y, z128 *work, int64_t nsteps,
                                 cudaGraphExec_t *graph);

@@ -66,6 +66,9 @@ struct StepArgs {
   typename real_of<Z>::type dt, dt_2, dt_6, dt_62;  // dt, dt/2, dt/6, dt/6*2
   int64_t *step;
   int64_t rend;  // last step of this problem's action (batched stepping)
+  // Rows [row0, row1) of the one-thread-per-row complex128 stage kernel
+  // (k_rstage); 0 and N except when stage 4 of a step runs in row slabs.
+  int64_t row0, row1;
   // Forcing block (complex64 block-row stages only): the half-step forcings
   // of a block of steps, synthesised ahead by k_forcing_block, slot 2s at
   // the half step and 2s+1 at the end of the block's step s; nullptr when
@@ -756,7 +759,7 @@ __global__ void __launch_bounds__(kRowThreads) k_rstage(const StepArgs<Z> P) {
   extern __shared__ unsigned char smem_raw[];
   Z *e2 = reinterpret_cast<Z *>(smem_raw);  // phasor rows of this step (stage 1)
   Z *e3 = e2 + P.Nw;
-  const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t n = P.row0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t i = (S == 1) ? P.step[0] : P.step[1];
   if (S == 1) {
     if (P.Fh) {
@@ -769,7 +772,7 @@ __global__ void __launch_bounds__(kRowThreads) k_rstage(const StepArgs<Z> P) {
     }
     __syncthreads();
   }
-  if (n >= P.N) return;
+  if (n >= P.row1) return;
   if (S == 1 && n == 0) P.step[1] = i;
   const Z *x = (S == 1) ? P.y : (S == 2) ? P.zA : (S == 3) ? P.zB : P.zA;
   const Z *addv = (S == 1 || S == 4) ? P.F3 : P.F2;
@@ -936,6 +939,8 @@ static StepArgs<Z> make_args(rsvdt_ctx *ctx, int dir, bool forced) {
   P.dt_62 = (Rl)(dt / 6 * 2);
   P.step = ctx->d_step;
   P.rend = INT64_MAX;
+  P.row0 = 0;
+  P.row1 = P.N;
   P.fblk = nullptr;
   return P;
 }
@@ -1063,7 +1068,7 @@ static void launch_bstage(int stage, const StepArgs<Z> &P, cudaStream_t st) {
   const int g = grid_for(warps * 32, kRowThreads);
   const size_t sm = sizeof(Z) * 2 * (P.Nw > 0 ? P.Nw : 1);
   if constexpr (sizeof(Z) == 16) {
-    const int gr = grid_for(P.N, kRowThreads);
+    const int gr = grid_for(P.row1 - P.row0, kRowThreads);
     switch (stage) {
       case 1: launch_pdl(k_rstage<Z, K, 1>, gr, kRowThreads, sm, st, P); break;
       case 2: launch_pdl(k_rstage<Z, K, 2>, gr, kRowThreads, 0, st, P); break;
@@ -1294,20 +1299,60 @@ static rsvdt_status run_steps_t(rsvdt_ctx *ctx, int dir, int64_t i0, int64_t nst
 // 1 and 2 (F3, the forcing at the step's end, is final from there on):
 // rsvdt_rk4_steps reads F3 back on a second stream meanwhile. Row kernels
 // (one lane per row) only.
-rsvdt_status run_last_step_split(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1) {
+// Row slabs stage 4 of a step can run in: the one-thread-per-row complex128
+// kernel takes a row range (k_rstage: 5x5 block rows, k in its list);
+// other kernels run whole (1 slab).
+template <class Z>
+static int stage4_slabs(const StepArgs<Z> &P, int want) {
+  if constexpr (sizeof(Z) != 16) return 1;
+  if (P.bs != 5 || P.fblk) return 1;
+  switch (P.K) {
+    case 1: case 2: case 4: case 6: case 8: case 10: case 16: return want;
+    default: return 1;
+  }
+}
+
+// Stages 2-4 of a step, stage 4 in nslab row slabs with slab_done[s]
+// recorded after slab s (rows N s / nslab .. N (s+1) / nslab).
+template <class Z>
+static int64_t launch_stages_234(rsvdt_ctx *ctx, StepArgs<Z> P, int nslab, cudaEvent_t *slab_done) {
+  launch_stage(2, P, ctx->stream);
+  launch_stage(3, P, ctx->stream);
+  if (!slab_done) {
+    launch_stage(4, P, ctx->stream);
+    return 3;
+  }
+  const int64_t N = P.N;
+  for (int s = 0; s < nslab; ++s) {
+    P.row0 = N * s / nslab;
+    P.row1 = N * (s + 1) / nslab;
+    launch_stage(4, P, ctx->stream);
+    cudaEventRecord(slab_done[s], ctx->stream);
+  }
+  return 2 + nslab;
+}
+
+int stage4_slab_count(rsvdt_ctx *ctx, int dir, int prec, int want) {
+  if (prec == RSVDT_PREC_C64) return stage4_slabs(make_args<z64>(ctx, dir, true), want);
+  return stage4_slabs(make_args<z128>(ctx, dir, true), want);
+}
+
+rsvdt_status run_last_step_split(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1,
+                                 int nslab, cudaEvent_t *slab_done) {
   k_set_step<<<1, 1, 0, ctx->stream>>>(ctx->d_step, i);
+  int64_t n = 2;
   if (prec == RSVDT_PREC_C64) {
     auto P = make_args<z64>(ctx, dir, true);
     launch_stage(1, P, ctx->stream);
     cudaEventRecord(after_stage1, ctx->stream);
-    for (int s = 2; s <= 4; ++s) launch_stage(s, P, ctx->stream);
+    n += launch_stages_234(ctx, P, 1, nullptr);
   } else {
     auto P = make_args<z128>(ctx, dir, true);
     launch_stage(1, P, ctx->stream);
     cudaEventRecord(after_stage1, ctx->stream);
-    for (int s = 2; s <= 4; ++s) launch_stage(s, P, ctx->stream);
+    n += launch_stages_234(ctx, P, nslab, slab_done);
   }
-  ctx->launches += 5;
+  ctx->launches += n;
   return cuda_ok(ctx, cudaGetLastError(), "rk4 step") ? RSVDT_OK : RSVDT_ERR_CUDA;
 }
 
@@ -1658,14 +1703,14 @@ static rsvdt_status forcing_ahead_t(rsvdt_ctx *ctx, int dir, int64_t i) {
 }
 
 template <class Z>
-static rsvdt_status first_step_rest_t(rsvdt_ctx *ctx, int dir, int64_t i, cudaEvent_t after_stage1) {
+static rsvdt_status first_step_rest_t(rsvdt_ctx *ctx, int dir, int64_t i, cudaEvent_t after_stage1, int nslab,
+                                      cudaEvent_t *slab_done) {
   auto P = make_args<Z>(ctx, dir, true);
   const int64_t NK = P.N * P.K;
   k_set_step<<<1, 1, 0, ctx->stream>>>(ctx->d_step, i);
   k_stage1_pre<Z><<<grid_for(NK, 256), 256, 0, ctx->stream>>>(P, (const Z *)ctx->cl_fbuf);
   if (after_stage1) cudaEventRecord(after_stage1, ctx->stream);
-  for (int s = 2; s <= 4; ++s) launch_stage(s, P, ctx->stream);
-  ctx->launches += 5;
+  ctx->launches += 2 + launch_stages_234(ctx, P, nslab, slab_done);
   return cuda_ok(ctx, cudaGetLastError(), "first step") ? RSVDT_OK : RSVDT_ERR_CUDA;
 }
 
@@ -1676,9 +1721,10 @@ rsvdt_status launch_forcing_ahead(rsvdt_ctx *ctx, int dir, int prec, int64_t i) 
 
 // The rest of step i once the state is on the device: stage 1 from the
 // buffered forcing (after_stage1, if given, recorded after it), stages 2-4.
-rsvdt_status launch_first_step_rest(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1) {
-  return prec == RSVDT_PREC_C64 ? first_step_rest_t<z64>(ctx, dir, i, after_stage1)
-                                : first_step_rest_t<z128>(ctx, dir, i, after_stage1);
+rsvdt_status launch_first_step_rest(rsvdt_ctx *ctx, int dir, int prec, int64_t i, cudaEvent_t after_stage1,
+                                    int nslab, cudaEvent_t *slab_done) {
+  return prec == RSVDT_PREC_C64 ? first_step_rest_t<z64>(ctx, dir, i, after_stage1, 1, nullptr)
+                                : first_step_rest_t<z128>(ctx, dir, i, after_stage1, nslab, slab_done);
 }
 
 // Whether the cluster engine runs this context's steps (and its shape).

@@ -153,6 +153,38 @@ def test_rk4_steps_with_row_kernels_match_oracle(built_lib, nsteps):
     ctx.close()
 
 
+@pytest.mark.parametrize("nsteps", [1, 9])
+def test_rk4_steps_block_rows_match_oracle(built_lib, nsteps):
+    """rsvdt_rk4_steps on the complex128 block-row kernels (k_rstage), whose
+    last step runs stage 4 in row slabs, each slab's rows of y downloaded
+    while the next computes: y and F3 against the oracle."""
+    import rsvdt
+    bcsr = synth.op3d_blocks(n=4, shift=0.5, seed=8)
+    A = synth.bcsr_to_csr(*bcsr)
+    cfg = dict(w=0.5, Nw=8, dt=0.05, TransientLength=2 * np.pi / 0.5)
+    k = 10
+    p = rsvdt.default_params(k=k, q=0, Nw=cfg["Nw"], w=cfg["w"], dt=cfg["dt"],
+                             TransientLength=cfg["TransientLength"], Display=0)
+    ctx = rsvdt.Context(p)
+    ctx.set_operator_bcsr(*bcsr)
+    ctx.set_step_engine(rsvdt.ENGINE_STAGES)
+    ctx.set_lanes_per_row(1)
+    N, nwe = A.shape[0], ctx.grid().Nw_eff
+    F = synth.complex_normal(N, k * nwe, 31)
+    y0 = synth.complex_normal(N, k, 32)
+    F30 = synth.complex_normal(N, k, 33)
+    ctx.set_sketch(F)
+    orc = oracle.Oracle(A, cfg["Nw"], cfg["w"], cfg["dt"], cfg["TransientLength"])
+    for d in (1, 0):
+        y, F3 = ctx.rk4_steps(d, 3, nsteps, y0.copy(), F30.copy())
+        for ik in range(k):
+            Fk = F[:, [iw * k + ik for iw in range(nwe)]]
+            yo, F3o = orc.rk4_steps(d, Fk, 3, nsteps, y0[:, ik], F30[:, ik])
+            assert rel(y[:, ik], yo) < 1e-11 and rel(F3[:, ik], F3o) < 1e-11, (d, ik)
+    orc.close()
+    ctx.close()
+
+
 @pytest.mark.parametrize("direction,tr", [(1, False), (0, False), (1, True), (0, True)])
 def test_action_matches_oracle(built_lib, direction, tr):
     """One resolvent action (TSActionRK4 + DFT or transient removal)."""
