@@ -322,7 +322,7 @@ def ttg_gl1(q_max: int = 8):
 def ttg_3d24(q_max: int = 24, seed: int = 99, k: int = 16):
     """Time to gains on the five-field 3D operator at 24^3 (N = 69,120, the
     3D64 configuration's 32 frequencies, diagonal W, recorded spectral
-    shift, dt at the RK4 stability limit) against the exact resolvent gains
+    shift, dt at 0.7 of the RK4 stability limit) against the exact resolvent gains
     of tests/golden/exact_gains_op3d24.npz (sparse LU + Lanczos, FP64), with
     k = 16 test vectors: the leading singular values of this operator's
     resolvent are close together at every frequency, and with the
@@ -360,29 +360,35 @@ def ttg_3d24(q_max: int = 24, seed: int = 99, k: int = 16):
     # periods leave 2e-3 of it, three 8e-5. Transient removal is not in the
     # plans: its FP64 Galerkin step costs more per action here than a third
     # period does. At the stability-limit dt the RK4 response itself is off
-    # by about 1e-3 at the highest frequencies (w dt = 0.68): measured, the
-    # complex64 run levels off near 1.4e-3 by q = 20.
-    plans = [(3, 0, 1.0)]
+    # by about 1e-3 at the highest frequencies (w dt = 0.68; RK4's error
+    # grows as (w dt)^4): measured, the complex64 run levels off near 1.4e-3
+    # by q = 20 and never meets the tolerance. With dt at 0.7 of the limit
+    # (w dt = 0.48) it meets it at q = 22 (9.7e-4; 1.3e-3 at q = 21), with
+    # 0.5 at q = 24; the error falls about 20% per power iteration near
+    # there. The plan starts at q = 22 and searches up or down from there,
+    # since a search from q = 0 would cost minutes of complex128 runs.
+    plans = [(3, 0, 0.7)]
     return ttg_forms(runner, lambda S, j: gain_rel_err(S, Sx, j), [float(Sx[0].min()), float(Sx[0].max())],
-                     plans, q_max, budget_s=150.0, workload=
+                     plans, q_max, budget_s=300.0, q_start={(3, 0, 0.7): 22}, workload=
                      f"3D24: N={wl.N} five-field operator (5x5 blocks), k={k}, Nw=32, diagonal W, shift "
-                     f"{wl.meta['shift']:.6g} ({wl.meta['shift_method']}), dt={wl.dt_in:.4g} (RK4 limit); exact "
-                     "gains: sparse LU + Lanczos (tests/golden/exact_gains_op3d24.npz)")
+                     f"{wl.meta['shift']:.6g} ({wl.meta['shift_method']}), dt={wl.dt_in:.4g} (RK4 limit) x 0.7; "
+                     "exact gains: sparse LU + Lanczos (tests/golden/exact_gains_op3d24.npz)")
 
 
-def ttg_followup(run, err, plans, q_found: dict, q_max: int, log=None, deadline: float = float("inf")):
-    """ttg_search for a further form, given the q at which a first form met
-    the tolerance per plan (the sketch sets the error, not the arithmetic:
-    the forms' errors agree to far below the tolerance). Per plan the run
-    starts at one q below, goes up until the tolerance is met, and down
-    while it still is, so that every reported q is the form's own smallest
-    one; plans the first form never met are skipped."""
+def ttg_followup(run, err, plans, q_start: dict, q_max: int, log=None, deadline: float = float("inf")):
+    """ttg_search from a given q per plan: the run starts at q_start[plan],
+    goes up until the tolerance is met, and down while it still is, so that
+    every reported q is the form's own smallest one; plans without a start
+    are skipped. Used for the further forms, starting one q below the q at
+    which the first form met the tolerance (the sketch sets the error, not
+    the arithmetic: the forms' errors agree to far below the tolerance), and
+    for a first form whose plan comes with a starting q."""
     best, trace = None, []
     for periods, tr, dtf in plans:
-        qf = q_found.get((periods, tr, dtf))
-        if qf is None:
+        q = q_start.get((periods, tr, dtf))
+        if q is None:
             continue
-        q = max(0, qf - 1)
+        q = max(0, q)
         met = {}
         while 0 <= q <= q_max and q not in met and time.perf_counter() <= deadline:
             t, S = run(q, periods, tr, dtf)
@@ -409,12 +415,14 @@ def ttg_followup(run, err, plans, q_found: dict, q_max: int, log=None, deadline:
     return best, trace
 
 
-def ttg_forms(runner, err, sigma1_range, plans, q_max, workload, forms=None, budget_s: float = 180.0):
+def ttg_forms(runner, err, sigma1_range, plans, q_max, workload, forms=None, budget_s: float = 180.0,
+              q_start: dict | None = None):
     """Time to gains of every form: the first form (the fastest per run,
-    complex64) is searched over all plans and q (ttg_search), the others
-    around the q it needed (ttg_followup). Each form is run once untimed
-    first (kernel loading). `forms`: (name, precision) pairs, the plain form
-    named plain_c128. The first form's search stops after half of budget_s
+    complex64) is searched over all plans and q (ttg_search), or from
+    q_start[plan] up or down when given (ttg_followup), the others around
+    the q it needed (ttg_followup). Each form is run once untimed first
+    (kernel loading). `forms`: (name, precision) pairs, the plain form named
+    plain_c128. The first form's search stops after half of budget_s
     seconds, every further form's after its share of the rest."""
     import rsvdt
 
@@ -423,8 +431,11 @@ def ttg_forms(runner, err, sigma1_range, plans, q_max, workload, forms=None, bud
     out = {"workload": workload, "tolerance": TTG_TOL,
            "search": "per plan (transient periods, transient removal, dt factor): the smallest q with "
                      "max_{w, j<=3} |s_j - sigma_j| / sigma_j <= 1e-3; the fastest such run per form (first "
-                     "form: q = 0, 1, ...; the others from one q below the first form's q, up or down)",
+                     "form: q = 0, 1, ..., or from the plan's starting q up or down; the others from one q "
+                     "below the first form's q, up or down)",
            "plans": [list(pl) for pl in plans], "sigma1_range": sigma1_range}
+    if q_start:
+        out["q_start"] = {",".join(str(x) for x in pl): q for pl, q in q_start.items()}
     q_found = None
     t_start = time.perf_counter()
     for fi, (name, prec) in enumerate(forms):
@@ -439,14 +450,18 @@ def ttg_forms(runner, err, sigma1_range, plans, q_max, workload, forms=None, bud
             print(f"ttg {n} {r}", file=sys.stderr, flush=True)
 
         if q_found is None:
-            best, trace = ttg_search(run, err, plans, q_max, log=log, deadline=deadline)
+            if q_start:
+                best, trace = ttg_followup(run, err, plans, q_start, q_max, log=log, deadline=deadline)
+            else:
+                best, trace = ttg_search(run, err, plans, q_max, log=log, deadline=deadline)
             q_found = {}
             for r in trace:
                 key = (r["periods"], r["tr"], r["dt_factor"])
                 if r["err_j<=3"] <= TTG_TOL and key not in q_found:
                     q_found[key] = r["q"]
         else:
-            best, trace = ttg_followup(run, err, plans, q_found, q_max, log=log, deadline=deadline)
+            best, trace = ttg_followup(run, err, plans, {pl: q - 1 for pl, q in q_found.items()}, q_max, log=log,
+                                       deadline=deadline)
         out[name] = {"best": best, "trace": trace}
         if trace:
             lo = min(trace, key=lambda r: r["err_j<=3"])
@@ -1038,6 +1053,9 @@ def summarize(out):
             if b:
                 sm[f"ttg_{key}_{form}_s"] = b["s"]
                 sm[f"ttg_{key}_{form}_q"] = b["q"]
+    ratios = [(d.get("ratio_plain_over_chosen"), key) for key, d in ttg.items() if d and d.get("ratio_plain_over_chosen")]
+    if ratios:
+        sm["ttg_best_ratio"], sm["ttg_best_workload"] = max(ratios)
     lrn = out.get("learned_sketch") or {}
     for name in ("learned", "random"):
         scan = lrn.get(f"{name}_q_scan") or []
