@@ -1120,6 +1120,30 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def profile_case(n: int):
+    """The complex64 forcing-block step of the five-field operator on an n^3
+    grid, launch for launch the same every run, so that a profiler can pick
+    kernels by position: 3 warm-up steps (the forcing block of the first 16
+    steps, then 4 stage launches per step), then rsvdt_rk4_profile_ex over 2
+    steps (one forcing block for both, then 8 stage launches). Prints the
+    event times of the profiled steps."""
+    import rsvdt
+    from rsvdt import workloads
+
+    wl = workloads.make_3d(n=n)
+    ctx = rsvdt.Context(wl.params(precision=rsvdt.PREC_C64))
+    ctx.set_operator_bcsr(*wl.bcsr)
+    ctx.random_sketch(1234)
+    ctx.rk4_reset(rsvdt.DIRECT)
+    ctx.rk4_advance(rsvdt.DIRECT, 1, 3)
+    ctx.synchronize()
+    t = ctx.rk4_profile_ex(rsvdt.DIRECT, 4, 2)
+    print(json.dumps({"profile_case": f"3D{n} complex64 forcing-block step", "N": wl.N, "k": wl.k, "Nw": wl.Nw,
+                      "forcing_block": ctx.forcing_block(), "stage_ms_2_steps": [round(x, 4) for x in t[:4]],
+                      "forcing_block_ms": round(t[4], 4)}))
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1141,11 +1165,18 @@ def main():
                     help="run the precision form on the n^3 operator in capacity mode (128: the 10.5M-row case)")
     ap.add_argument("--large-periods", type=float, default=1.0, help="transient periods of the --large-n runs")
     ap.add_argument("--large-full", action="store_true", help="run the whole complex128 sequence in --large-n too")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="only the complex64 forcing-block step on the --n grid, for a profiler: 3 warm-up steps "
+                         "(13 launches: one forcing block, 12 stages), then one forcing block for 2 steps and "
+                         "their 8 stages")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.profile_case:
+        profile_case(args.n)
         return
 
     import torch

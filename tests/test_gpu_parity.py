@@ -290,8 +290,9 @@ def test_run_matches_oracle(built_lib, q, tr):
     ctx.run()
     U, V, S = ctx.get_results()
     Uo, Vo, So = make_oracle(A, cfg, tr=tr).run(F, q)
-    assert np.abs(S - So).max() / So.max() < GAIN_TOL
-    assert (np.abs(S - So) / So).max() < 1e-7
+    # Per (frequency, j) relative error of every gain.
+    rel_gain = np.abs(S - So) / So
+    assert rel_gain.max() < GAIN_TOL, rel_gain.max(axis=1)
     assert angles(U, Uo, k, g.Nw_eff, 1).max() < ANGLE_TOL
     assert angles(V, Vo, k, g.Nw_eff, 1).max() < ANGLE_TOL
     ctx.close()
