@@ -1280,7 +1280,10 @@ def main():
     parity = {}
     if rank == 0 and not args.no_parity:
         parity["steps_" + wl.name] = parity_steps(wl, ctx, ctx64, threads)
+    # Both step contexts are done: their device memory (about 25 GB) goes
+    # back before the side experiments (the 128^3 case needs all of it).
     ctx64.close()
+    ctx.close()
     eqq = None
     if rank == 0 and args.equal_q:
         eqq = equal_q_speedup(args.ttg_n)
@@ -1307,6 +1310,7 @@ def main():
         gl1 = gl1_form(min(os.cpu_count() or 1, 10))
     large = None
     if rank == 0 and args.large_n:
+        torch.cuda.empty_cache()  # the DGEMM probe's cached blocks
         large = large_precision_form(n=args.large_n, periods=args.large_periods, full_c128=args.large_full)
 
     cpu = None
@@ -1316,7 +1320,6 @@ def main():
         cpu = {"value": round(b["step"] / t_cpu / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                "sample": f"2 steps x {wl.k} test vectors of the same 3D64 step, row loops on {threads} threads "
                          f"({t_cpu:.2f} s/step); C restatement of SourceCode/TSRK4.c"}
-    ctx.close()
 
     def gbs(nbytes, ms):
         return nbytes / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
