@@ -454,11 +454,11 @@ def ttg_forms(runner, err, sigma1_range, plans, q_max, workload, forms=None, bud
                 best, trace = ttg_followup(run, err, plans, q_start, q_max, log=log, deadline=deadline)
             else:
                 best, trace = ttg_search(run, err, plans, q_max, log=log, deadline=deadline)
-            q_found = {}
+            q_found = {}  # per plan, the smallest q that met the tolerance
             for r in trace:
                 key = (r["periods"], r["tr"], r["dt_factor"])
-                if r["err_j<=3"] <= TTG_TOL and key not in q_found:
-                    q_found[key] = r["q"]
+                if r["err_j<=3"] <= TTG_TOL:
+                    q_found[key] = min(q_found.get(key, r["q"]), r["q"])
         else:
             best, trace = ttg_followup(run, err, plans, {pl: q - 1 for pl, q in q_found.items()}, q_max, log=log,
                                        deadline=deadline)
