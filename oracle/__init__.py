@@ -201,11 +201,29 @@ def svd_all_freqs(Y: np.ndarray, k: int):
 
 
 def freq_of(iw: int, Nw: int, w: float, real_op: bool = False) -> float:
-    """Angular frequency of column block iw: iw*w for iw < Nw/2, (iw - Nw)*w
-    otherwise (the ordering of SourceCode/CreateDFTiDFTMats.c:46-52)."""
-    if real_op or iw <= Nw // 2 - 1:
+    """Angular frequency of column block iw: iw*w up to Nw/2 - 1 (even Nw)
+    or (Nw - 1)/2 (odd Nw), (iw - Nw)*w above (the ordering of
+    SourceCode/CreateDFTiDFTMats.c:46-52); iw*w for a real operator."""
+    half = Nw // 2 - 1 if Nw % 2 == 0 else (Nw - 1) // 2
+    if real_op or iw <= half:
         return iw * w
     return (iw - Nw) * w
+
+
+def rk4_tone_response(lam, om: float, dt: float):
+    """Steady-state answer H of forced RK4 (SourceCode/TSRK4.c:18-47: the
+    forcing at t, t + dt/2 twice and t + dt) on y' = lam y + e^{i om t}:
+    y_n = H e^{i om n dt} with H = dt G / (e^{i om dt} - P(lam dt)), P the
+    RK4 amplification polynomial and G the stages' forcing sum. For a
+    diagonal operator the direct action is e^{i om (Nt + R) dt} H F
+    exactly, once the transient has decayed."""
+    z = np.asarray(lam) * dt
+    a, b = np.exp(0.5j * om * dt), np.exp(1j * om * dt)
+    P = 1 + z + z ** 2 / 2 + z ** 3 / 6 + z ** 4 / 24
+    k2 = z / 2 + a
+    k3 = z / 2 * k2 + a
+    k4 = z * k3 + b
+    return dt * (1 + 2 * k2 + 2 * k3 + k4) / 6 / (b - P)
 
 
 def dense_resolvent_svd(A, omegas, k: int, Wq=None, Wf_inv=None, B=None, Cm=None):

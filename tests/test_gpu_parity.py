@@ -619,3 +619,34 @@ def test_gl1_config_matches_oracle(built_lib, q, tr):
     assert angles(U, Uo, k, 64, 1).max() < ANGLE_TOL
     assert angles(V, Vo, k, 64, 1).max() < ANGLE_TOL
     ctx.close()
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-11), (1, 1e-5)])  # complex128, complex64 form
+def test_direct_action_is_the_rk4_transfer_function(built_lib, prec, tol):
+    """The direct action of a diagonal operator on the GPU against the
+    closed form of forced RK4 (oracle.rk4_tone_response: each row a scalar
+    ODE; Y[:, iw k + j] = e^{i w (Nt + R) dt} H(lam, w) F[:, iw k + j] once
+    the transient has decayed), independently of the C restatement:
+    complex128 to rounding, the complex64 form to its FP32 state."""
+    import rsvdt
+    N, w, Nw, k = 12, 0.1, 16, 2
+    rng = np.random.default_rng(8)
+    lam = -1.0 - 2.0 * rng.random(N) + 1j * rng.uniform(-3, 3, N)
+    A = sp.diags(lam).tocsr()
+    cfg = dict(w=w, Nw=Nw, dt=0.15, TransientLength=2 * np.pi / w)
+    ctx = make_ctx(A, cfg, k=k, prec=prec)
+    g = ctx.grid()
+    z = lam * g.dt
+    assert g.Nt == g.Ns and (np.abs(1 + z + z ** 2 / 2 + z ** 3 / 6 + z ** 4 / 24) ** g.Nt < 1e-15).all()
+    F = synth.complex_normal(N, k * Nw, 10)
+    ctx.set_sketch(F)
+    ctx.action(rsvdt.DIRECT)
+    Y = ctx.get_block()
+    ctx.close()
+    for iw in range(Nw):
+        om = oracle.freq_of(iw, Nw, w)
+        H = oracle.rk4_tone_response(lam, om, g.dt)
+        for j in range(k):
+            c = iw * k + j
+            expect = np.exp(1j * om * (g.Nt + g.ResRatio) * g.dt) * H * F[:, c]
+            assert np.abs(Y[:, c] - expect).max() / np.abs(expect).max() < tol, (iw, j)

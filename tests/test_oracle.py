@@ -196,3 +196,41 @@ def test_sparse_resolvent_oracle_matches_the_dense_one():
             for X, Xd in ((U, Ud), (V, Vd)):
                 c = abs(np.vdot(Xd[j][:, 0], X[j][:, 0]))
                 assert abs(c - 1) < 1e-8
+
+
+@pytest.mark.parametrize("Nw", [16, 7])
+def test_direct_action_is_the_rk4_transfer_function(Nw):
+    """For a diagonal operator the direct action is known in closed form:
+    each row is a scalar ODE y' = lam y + f(t), and forced RK4 with the
+    forcing at t, t + dt/2 (twice) and t + dt (SourceCode/TSRK4.c:18-47)
+    answers a tone e^{i w t} in steady state with y_n = H e^{i w n dt},
+        H = dt G / (e^{i w dt} - P(z)),  z = lam dt,
+        P(z) = 1 + z + z^2/2 + z^3/6 + z^4/24,
+        G = (k1 + 2 k2 + 2 k3 + k4) / 6,  k1 = 1, k2 = z/2 + a,
+        k3 = (z/2) k2 + a,  k4 = z k3 + b,  a = e^{i w dt/2}, b = e^{i w dt}.
+    The idft's 1/Ns, the DFT's ResRatio and the sample times Nt + R (p + 1)
+    of SaveSnapshots (SourceCode/SaveSnapshots.c:19-29) then give
+    Y[:, iw] = e^{i w (Nt + R) dt} H F[:, iw] exactly, once the transient
+    (a factor |P(z)| per step) has decayed: the whole forcing, stepping,
+    sampling and DFT chain of the oracle to rounding, not to RK4 accuracy."""
+    import scipy.sparse as sp
+
+    N, w, dt_in = 12, 0.1, 0.15
+    T = 2 * np.pi / w
+    rng = np.random.default_rng(8)
+    lam = -1.0 - 2.0 * rng.random(N) + 1j * rng.uniform(-3, 3, N)
+    A = sp.diags(lam).tocsr()
+    o = oracle.Oracle(A, Nw, w, dt_in, T)
+    z = lam * o.dt
+    # One transient period: the homogeneous part has decayed below rounding.
+    assert o.Nt == o.Ns and (np.abs(1 + z + z ** 2 / 2 + z ** 3 / 6 + z ** 4 / 24) ** o.Nt < 1e-15).all()
+    F = synth.complex_normal(N, Nw, 9)
+    Y = o.ts_action(1, F)
+    dt = o.dt
+    for iw in range(Nw):
+        om = oracle.freq_of(iw, Nw, w)
+        H = oracle.rk4_tone_response(lam, om, dt)
+        expect = np.exp(1j * om * (o.Nt + o.R) * dt) * H * F[:, iw]
+        err = np.abs(Y[:, iw] - expect).max() / np.abs(expect).max()
+        assert err < 1e-12, (iw, om, err)
+    o.close()
