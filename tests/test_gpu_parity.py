@@ -622,12 +622,15 @@ def test_gl1_config_matches_oracle(built_lib, q, tr):
 
 
 @pytest.mark.parametrize("prec,tol", [(0, 1e-11), (1, 1e-5)])  # complex128, complex64 form
-def test_direct_action_is_the_rk4_transfer_function(built_lib, prec, tol):
-    """The direct action of a diagonal operator on the GPU against the
-    closed form of forced RK4 (oracle.rk4_tone_response: each row a scalar
-    ODE; Y[:, iw k + j] = e^{i w (Nt + R) dt} H(lam, w) F[:, iw k + j] once
-    the transient has decayed), independently of the C restatement:
-    complex128 to rounding, the complex64 form to its FP32 state."""
+@pytest.mark.parametrize("direction", [1, 0])
+def test_actions_are_the_rk4_transfer_function(built_lib, prec, tol, direction):
+    """The actions of a diagonal operator on the GPU against the closed
+    form of forced RK4 (oracle.rk4_tone_response: each row a scalar ODE),
+    independently of the C restatement, once the transient has decayed:
+    direct Y[:, iw k + j] = e^{i w (Nt + R) dt} H(lam, w) F[:, iw k + j],
+    adjoint (A^H, time-reversed forcing, samples in reverse slot order)
+    e^{-i w Nt dt} conj(H) F; complex128 to rounding, the complex64 form to
+    its FP32 state."""
     import rsvdt
     N, w, Nw, k = 12, 0.1, 16, 2
     rng = np.random.default_rng(8)
@@ -640,13 +643,17 @@ def test_direct_action_is_the_rk4_transfer_function(built_lib, prec, tol):
     assert g.Nt == g.Ns and (np.abs(1 + z + z ** 2 / 2 + z ** 3 / 6 + z ** 4 / 24) ** g.Nt < 1e-15).all()
     F = synth.complex_normal(N, k * Nw, 10)
     ctx.set_sketch(F)
-    ctx.action(rsvdt.DIRECT)
+    ctx.action(direction)
     Y = ctx.get_block()
     ctx.close()
     for iw in range(Nw):
         om = oracle.freq_of(iw, Nw, w)
         H = oracle.rk4_tone_response(lam, om, g.dt)
+        if direction == rsvdt.DIRECT:
+            resp = np.exp(1j * om * (g.Nt + g.ResRatio) * g.dt) * H
+        else:
+            resp = np.exp(-1j * om * g.Nt * g.dt) * np.conj(H)
         for j in range(k):
             c = iw * k + j
-            expect = np.exp(1j * om * (g.Nt + g.ResRatio) * g.dt) * H * F[:, c]
+            expect = resp * F[:, c]
             assert np.abs(Y[:, c] - expect).max() / np.abs(expect).max() < tol, (iw, j)

@@ -199,7 +199,7 @@ def test_sparse_resolvent_oracle_matches_the_dense_one():
 
 
 @pytest.mark.parametrize("Nw", [16, 7])
-def test_direct_action_is_the_rk4_transfer_function(Nw):
+def test_actions_are_the_rk4_transfer_function(Nw):
     """For a diagonal operator the direct action is known in closed form:
     each row is a scalar ODE y' = lam y + f(t), and forced RK4 with the
     forcing at t, t + dt/2 (twice) and t + dt (SourceCode/TSRK4.c:18-47)
@@ -232,5 +232,16 @@ def test_direct_action_is_the_rk4_transfer_function(Nw):
         H = oracle.rk4_tone_response(lam, om, dt)
         expect = np.exp(1j * om * (o.Nt + o.R) * dt) * H * F[:, iw]
         err = np.abs(Y[:, iw] - expect).max() / np.abs(expect).max()
+        assert err < 1e-12, (iw, om, err)
+    # The adjoint action steps A^H with the forcing time-reversed (indices
+    # (-1 - m) mod 2 Ns, SourceCode/TSRK4.c:21-26) and stores the samples in
+    # reverse slot order (SourceCode/SaveSnapshots.c:24-26): the same
+    # algebra gives e^{-i w Nt dt} conj(H) F.
+    Ya = o.ts_action(0, F)
+    for iw in range(Nw):
+        om = oracle.freq_of(iw, Nw, w)
+        H = oracle.rk4_tone_response(lam, om, dt)
+        expect = np.exp(-1j * om * o.Nt * dt) * np.conj(H) * F[:, iw]
+        err = np.abs(Ya[:, iw] - expect).max() / np.abs(expect).max()
         assert err < 1e-12, (iw, om, err)
     o.close()
