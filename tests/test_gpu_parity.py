@@ -657,3 +657,28 @@ def test_actions_are_the_rk4_transfer_function(built_lib, prec, tol, direction):
             c = iw * k + j
             expect = resp * F[:, c]
             assert np.abs(Y[:, c] - expect).max() / np.abs(expect).max() < tol, (iw, j)
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-11), (1, 1e-5)])  # complex128, complex64 form
+def test_real_operator_action_is_the_rk4_transfer_function(built_lib, prec, tol):
+    """A real diagonal operator (the real-operator branch: Nw/2 non-negative
+    frequencies) on the GPU against the closed form of forced RK4."""
+    import rsvdt
+    N, w, Nw, k = 12, 0.1, 16, 2
+    lam = -1.0 - 2.0 * np.random.default_rng(8).random(N) + 0j
+    cfg = dict(w=w, Nw=Nw, dt=0.15, TransientLength=2 * np.pi / w)
+    ctx = make_ctx(sp.diags(lam).tocsr(), cfg, k=k, prec=prec)
+    g = ctx.grid()
+    assert g.Nw_eff == Nw // 2
+    F = synth.complex_normal(N, k * g.Nw_eff, 11)
+    ctx.set_sketch(F)
+    ctx.action(rsvdt.DIRECT)
+    Y = ctx.get_block()
+    ctx.close()
+    for iw in range(g.Nw_eff):
+        om = oracle.freq_of(iw, Nw, w, real_op=True)
+        resp = np.exp(1j * om * (g.Nt + g.ResRatio) * g.dt) * oracle.rk4_tone_response(lam, om, g.dt)
+        for j in range(k):
+            c = iw * k + j
+            expect = resp * F[:, c]
+            assert np.abs(Y[:, c] - expect).max() / np.abs(expect).max() < tol, (iw, j)

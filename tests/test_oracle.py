@@ -245,3 +245,24 @@ def test_actions_are_the_rk4_transfer_function(Nw):
         err = np.abs(Ya[:, iw] - expect).max() / np.abs(expect).max()
         assert err < 1e-12, (iw, om, err)
     o.close()
+
+
+def test_real_operator_action_is_the_rk4_transfer_function():
+    """A real diagonal operator takes the reference's real-operator branch
+    (Nw/2 non-negative frequencies, SourceCode/LNSStructure.c:37-44 and
+    CreateDFTiDFTMats.c:46-47,63-76); its direct action is the same closed
+    form, e^{i w (Nt + R) dt} H F, to rounding."""
+    import scipy.sparse as sp
+
+    N, w, Nw, dt_in = 12, 0.1, 16, 0.15
+    lam = -1.0 - 2.0 * np.random.default_rng(8).random(N) + 0j
+    o = oracle.Oracle(sp.diags(lam).tocsr(), Nw, w, dt_in, 2 * np.pi / w)
+    assert o.real_op and o.Nw_eff == Nw // 2
+    F = synth.complex_normal(N, Nw // 2, 9)
+    Y = o.ts_action(1, F)
+    for iw in range(Nw // 2):
+        om = oracle.freq_of(iw, Nw, w, real_op=True)
+        H = oracle.rk4_tone_response(lam, om, o.dt)
+        expect = np.exp(1j * om * (o.Nt + o.R) * o.dt) * H * F[:, iw]
+        assert np.abs(Y[:, iw] - expect).max() / np.abs(expect).max() < 1e-12, iw
+    o.close()
