@@ -682,3 +682,45 @@ def test_real_operator_action_is_the_rk4_transfer_function(built_lib, prec, tol)
             c = iw * k + j
             expect = resp * F[:, c]
             assert np.abs(Y[:, c] - expect).max() / np.abs(expect).max() < tol, (iw, j)
+
+
+# complex128 at q = 0 and 1; the complex64 form at q = 0 (its FP32 state
+# leaves mode errors near 1e-4 where two gains are close).
+@pytest.mark.parametrize("prec,q,gtol,mtol", [(0, 0, 1e-10, 1e-8), (0, 1, 1e-10, 1e-8), (1, 0, 1e-5, 1e-4)])
+def test_whole_run_of_a_diagonal_operator_is_exact(built_lib, prec, q, gtol, mtol):
+    """The whole sequence on the GPU with a full sketch (k = N) on a
+    diagonal operator with diagonal weights, against the closed form rather
+    than the restatement: gains = the sorted |a_n H_n b_n| (H the forced-RK4
+    answer, a = W_q^{1/2}, b = W_f^{-1/2}), V's columns e_n b_n, U's
+    columns e_n / a_n from q = 1 on (U is taken before the adjoint: at q = 0
+    it is the left singular basis of R F, which depends on the sketch)."""
+    import rsvdt
+    N, w, Nw = 12, 0.1, 16
+    rng = np.random.default_rng(8)
+    lam = -1.0 - 2.0 * rng.random(N) + 1j * rng.uniform(-3, 3, N)
+    vol = rng.uniform(0.5, 1.5, N)
+    a, b = np.sqrt(vol), 1 / np.sqrt(vol)
+    cfg = dict(w=w, Nw=Nw, dt=0.15, TransientLength=2 * np.pi / w)
+    ctx = make_ctx(sp.diags(lam).tocsr(), cfg, k=N, q=q, prec=prec)
+    ctx.set_weight(rsvdt.W_Q_SQRT, sp.diags(a + 0j).tocsr())
+    ctx.set_weight(rsvdt.W_F_SQRT_INV, sp.diags(b + 0j).tocsr())
+    ctx.set_weight(rsvdt.W_Q_SQRT_INV, sp.diags(1 / a + 0j).tocsr())
+    ctx.set_sketch(synth.complex_normal(N, N * Nw, 9))
+    ctx.run()
+    U, V, S = ctx.get_results()
+    dt = ctx.grid().dt
+    ctx.close()
+    for iw in range(Nw):
+        g = np.abs(a * oracle.rk4_tone_response(lam, oracle.freq_of(iw, Nw, w), dt) * b)
+        order = np.argsort(-g)
+        assert (np.abs(S[:, iw] - g[order]) / g[order]).max() < gtol, iw
+        for j in range(3):
+            n = order[j]
+            for M, scale, check in ((V, b[n], True), (U, 1 / a[n], q >= 1)):
+                if not check:
+                    continue
+                col = M[:, iw * N + j]
+                e = np.zeros(N)
+                e[n] = scale
+                c = np.vdot(e, col) / np.vdot(e, e)
+                assert abs(abs(c) - 1) < mtol and np.linalg.norm(col - c * e) / scale < mtol, (iw, j)

@@ -266,3 +266,52 @@ def test_real_operator_action_is_the_rk4_transfer_function():
         expect = np.exp(1j * om * (o.Nt + o.R) * o.dt) * H * F[:, iw]
         assert np.abs(Y[:, iw] - expect).max() / np.abs(expect).max() < 1e-12, iw
     o.close()
+
+
+def _diag_run_expectation(lam, a, b, om, dt, k):
+    """Gains and mode rows of W_q^{1/2} R(w) W_f^{-1/2} for a diagonal
+    operator and diagonal weights, R the forced-RK4 answer diag(H): the
+    singular values are |a_n H_n b_n| sorted, the singular vectors unit
+    vectors e_n; after the inverse weights of SourceCode/SVDAllFreqs.c:63-64
+    the j-th U and V columns are e_n / a_n and e_n b_n (up to a phase)."""
+    g = np.abs(a * oracle.rk4_tone_response(lam, om, dt) * b)
+    order = np.argsort(-g)[:k]
+    return g[order], order
+
+
+def test_whole_run_of_a_diagonal_operator_is_exact():
+    """The whole sequence of SourceCode/main.c:134-144 (actions, QR, SVD
+    before the adjoint, StoreU, adjoint action, SVD, inverse weights) with a
+    full sketch (k = N) on a diagonal operator with diagonal weights: the
+    gains are the sorted |a_n H_n b_n| to rounding at q = 0 and 1, V's
+    columns are e_n b_n; U (taken before the adjoint, SourceCode/StoreU.c:15)
+    is the left singular basis of R F, which is e_n / a_n once the sketch
+    is orthonormal, from q = 1 on."""
+    import scipy.sparse as sp
+
+    N, w, Nw, dt_in = 12, 0.1, 16, 0.15
+    rng = np.random.default_rng(8)
+    lam = -1.0 - 2.0 * rng.random(N) + 1j * rng.uniform(-3, 3, N)
+    vol = rng.uniform(0.5, 1.5, N)
+    a, b = np.sqrt(vol), 1 / np.sqrt(vol)  # W_q^{1/2} = W_f^{1/2} = diag(sqrt(vol))
+    for q in (0, 1):
+        o = oracle.Oracle(sp.diags(lam).tocsr(), Nw, w, dt_in, 2 * np.pi / w)
+        o.set_weight(3, sp.diags(a + 0j).tocsr())      # W_q^{1/2}
+        o.set_weight(0, sp.diags(b + 0j).tocsr())      # W_f^{-1/2}
+        o.set_weight(4, sp.diags(1 / a + 0j).tocsr())  # W_q^{-1/2}
+        F = synth.complex_normal(N, N * Nw, 9)
+        U, V, S = o.run(F, q)
+        for iw in range(Nw):
+            g, order = _diag_run_expectation(lam, a, b, oracle.freq_of(iw, Nw, w), o.dt, N)
+            assert (np.abs(S[:, iw] - g) / g).max() < 1e-12, (q, iw)
+            for j in range(3):
+                n = order[j]
+                for M, scale, check in ((V, b[n], True), (U, 1 / a[n], q >= 1)):
+                    if not check:
+                        continue
+                    col = M[:, iw * N + j]
+                    e = np.zeros(N)
+                    e[n] = scale
+                    c = np.vdot(e, col) / np.vdot(e, e)
+                    assert abs(abs(c) - 1) < 1e-9 and np.linalg.norm(col - c * e) / scale < 1e-9, (q, iw, j)
+        o.close()
