@@ -684,9 +684,10 @@ def test_real_operator_action_is_the_rk4_transfer_function(built_lib, prec, tol)
             assert np.abs(Y[:, c] - expect).max() / np.abs(expect).max() < tol, (iw, j)
 
 
-# complex128 at q = 0 and 1; the complex64 form at q = 0 (its FP32 state
-# leaves mode errors near 1e-4 where two gains are close).
-@pytest.mark.parametrize("prec,q,gtol,mtol", [(0, 0, 1e-10, 1e-8), (0, 1, 1e-10, 1e-8), (1, 0, 1e-5, 1e-4)])
+# complex128 to rounding; the complex64 form to its FP32 state (mode errors
+# up to about 1e-4 after a power iteration, where two gains are close).
+@pytest.mark.parametrize("prec,q,gtol,mtol", [(0, 0, 1e-10, 1e-8), (0, 1, 1e-10, 1e-8), (1, 0, 1e-5, 1e-4),
+                                              (1, 1, 1e-5, 1e-3)])
 def test_whole_run_of_a_diagonal_operator_is_exact(built_lib, prec, q, gtol, mtol):
     """The whole sequence on the GPU with a full sketch (k = N) on a
     diagonal operator with diagonal weights, against the closed form rather
